@@ -1,0 +1,226 @@
+/*
+ * tgvg.h -- C ABI of the GB300 (sm_103a) implementation of the TGVReconClaude
+ * Stage-5 (depth maps -> per-cube histograms) and Stage-6 (histogram-data-term
+ * primal-dual TGV over a Morton-ordered octree) hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns 0
+ * (TGVG_OK) or a negative TGVG_ERR_* code, and never throws.  A C++ caller that
+ * wants the reference's exception behaviour maps a nonzero code to
+ * std::runtime_error(tgvg_strerror(rc)).  Records are byte-identical to the
+ * reference's structs, so std::vector<OctreeCube>::data() etc. can be passed as
+ * they are.
+ *
+ * The reference interface each entry point replaces is cited as
+ * reference-path:line (paths inside the reference project).
+ */
+#ifndef TGVG_H
+#define TGVG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TGVG_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+#define TGVG_OK             0
+#define TGVG_ERR_INVALID   -1  /* bad argument (null pointer, size, depth outside 0..21, mode) */
+#define TGVG_ERR_CUDA      -2  /* a CUDA runtime call failed; tgvg_last_error() has the text  */
+#define TGVG_ERR_NOMEM     -3  /* device memory exhausted                                      */
+#define TGVG_ERR_UNSORTED  -4  /* streaming semantics need cubes sorted by Morton code         */
+#define TGVG_ERR_IO        -5  /* cannot open / short read / short write   (runtime_error)     */
+#define TGVG_ERR_FORMAT    -6  /* bad magic in a TGV1/TGVH/TGVT/TGVS file    (runtime_error)   */
+#define TGVG_ERR_TIMEOUT   -7  /* a bounded device wait ran out of iterations                  */
+#define TGVG_ERR_NODEVICE  -8  /* no CUDA device, or not an sm_103 part                        */
+#define TGVG_ERR_OVERLAP   -9  /* treetop leaves overlap                                       */
+
+/* ---- records (byte-identical to the reference) --------------------------- */
+
+/* OctreeCube, reference src/types.hpp:30-34 (16 B). code = {hi, lo} 63-bit Z-code
+ * of the cube's lower corner on the 2^21 fine grid. */
+typedef struct tgvg_cube {
+    uint32_t hi, lo;
+    float r_c;
+    int32_t depth;
+} tgvg_cube;
+
+/* TreetopLeaf, reference src/treetop.hpp:8-13 (20 B): inclusive index range. */
+typedef struct tgvg_leaf {
+    uint32_t hi, lo;
+    int32_t depth;
+    uint32_t first_idx, last_idx;
+} tgvg_leaf;
+
+/* TGVCube, reference src/tgv.hpp:12-17 (52 B). q in Voigt order xx yy zz xy xz yz. */
+typedef struct tgvg_state {
+    float u;
+    float v[3];
+    float p[3];
+    float q[6];
+} tgvg_state;
+
+/* Histogram rows are uint32[nbins]: nbins = 8 is CubeHistogram
+ * (reference src/histogram.hpp:10-19); nbins = 10 is the 10-bin extension. */
+
+/* One depth map as DepthMipmap holds it (reference src/histogram.hpp:22-38),
+ * without the texels. */
+typedef struct tgvg_camera {
+    float rt_inv[16];        /* camera<-world, ROW-major (DepthMipmap::Rt_inv)           */
+    float fx, fy, cx, cy;    /* level-0 intrinsics K(0,0), K(1,1), K(0,2), K(1,2)        */
+    int32_t width, height;   /* level-0 size                                             */
+    int32_t lidar;           /* nonzero: vote 5 instead of 1 (histogram.cpp:158)         */
+    int32_t reserved;        /* must be 0                                                */
+} tgvg_camera;
+
+/* TGVParams (reference src/tgv.hpp:24-28) plus the stopping extension. */
+typedef struct tgvg_params {
+    float alpha0;            /* weight on |e(v)|  (reference default 0.02)              */
+    float alpha1;            /* weight on |grad u - v| (reference default 0.04)         */
+    int32_t iters;           /* primal-dual iterations per level (maximum when tol > 0) */
+    int32_t init;            /* TGVG_INIT_*                                             */
+    float tol;               /* relative residual stop; 0 = fixed count (reference)     */
+    int32_t check_every;     /* residual evaluated every this many iterations           */
+} tgvg_params;
+
+#define TGVG_INIT_MEDIAN 0   /* u = median_indicator (reference, tgv.cpp:372-373) */
+#define TGVG_INIT_ZERO   1   /* u = 0 ("plain solver from a zero start")          */
+#define TGVG_INIT_GIVEN  2   /* u = caller array (learned warm start)             */
+
+#define TGVG_MODE_INMEM  0   /* tgv_minimize           (tgv.cpp:356-419) */
+#define TGVG_MODE_OC     1   /* tgv_minimize_oc        (tgv.cpp:423-511) */
+#define TGVG_MODE_STREAM 2   /* tgv_minimize_streaming (tgv.cpp:802-1070), all leaves batched */
+
+#define TGVG_MAX_LEVELS 22
+
+/* Per-solve counters. */
+typedef struct tgvg_stats {
+    int32_t n_levels;                    /* levels that had active cubes            */
+    int32_t min_depth, max_depth;
+    int32_t depth[TGVG_MAX_LEVELS];      /* depth of level slot k                   */
+    int64_t active[TGVG_MAX_LEVELS];     /* active cubes of level slot k            */
+    int32_t iters_run[TGVG_MAX_LEVELS];  /* iterations run (max over leaves)        */
+    double residual[TGVG_MAX_LEVELS];    /* last relative residual (max over leaves)*/
+    int64_t leaf_iters;                  /* sum over levels of active x iterations  */
+    int32_t kernel_launches;             /* kernels this call enqueued              */
+    int32_t reserved;
+    double setup_ms, iterate_ms, total_ms; /* device time of the phases             */
+    /* Per-launch timing of the iteration kernels on the level with the most
+     * active cubes (filled when tgvg_set_timing(ctx, 1) is on): summed CUDA
+     * event durations on the context stream and the launch count per kernel. */
+    int32_t kt_depth;
+    int32_t kt_launches;
+    int64_t kt_active;
+    double kt_dual_ms, kt_primal_ms;
+} tgvg_stats;
+
+typedef struct tgvg_ctx tgvg_ctx;
+
+/* ---- context ---------------------------------------------------------------
+ * One context per process and device: it owns the CUDA stream all calls run on
+ * and a grow-only pool of device buffers reused across calls.  Calls on one
+ * context are serialised by a mutex (the reference is single-threaded). */
+int tgvg_create(int device, tgvg_ctx** out);
+int tgvg_destroy(tgvg_ctx* ctx);
+const char* tgvg_strerror(int rc);
+const char* tgvg_last_error(tgvg_ctx* ctx);
+int tgvg_abi_version(void);
+/* The stream the context runs on (cudaStream_t as void*). */
+void* tgvg_stream(tgvg_ctx* ctx);
+/* Count of this library's kernels launched on the context since creation. */
+int64_t tgvg_kernel_count(tgvg_ctx* ctx);
+/* The 13 footprint thresholds the histogram kernel uses for the pyramid level
+ * (t[k] = smallest float >= 1 whose (int)log2f reaches k; t[0] = 1).  Host-only,
+ * needs no device: it reproduces `(int)std::log2(std::max(1.0f, footprint))`
+ * of histogram.cpp:99 without calling log2 on the GPU. */
+void tgvg_level_thresholds(float* t13);
+/* Turn per-launch event timing of the largest level's iteration kernels on (1)
+ * or off (0); results land in tgvg_stats.kt_*. */
+int tgvg_set_timing(tgvg_ctx* ctx, int on);
+
+/* ---- Stage 5: depth maps -> histograms ------------------------------------ */
+
+/* Pyramid geometry of a W x H map: writes (w, h) of every level into dims
+ * (2 entries per level, room for 13) and returns the level count
+ * (DepthMipmap::build level rule, reference src/histogram.cpp:42-53). */
+int tgvg_pyramid_dims(int32_t width, int32_t height, int32_t* dims);
+
+/* DepthMipmap::build (reference src/histogram.cpp:35-74) for ncam maps on the
+ * device.  base[c] is map c's level-0 texels (host); levels_out[c] (host,
+ * optional) receives all of map c's levels concatenated, level 0 first.
+ * Rt_inv stays with the caller (the reference computes it with Eigen). */
+int tgvg_build_pyramids(tgvg_ctx* ctx, const tgvg_camera* cams, int32_t ncam,
+                        const float* const* base, float* const* levels_out);
+
+/* compute_histograms (reference src/histogram.hpp:44-48, histogram.cpp:127-163).
+ * Host buffers in and out.  base[c]: map c's level-0 texels; the pyramids are
+ * built on the device.  out: n * nbins uint32.  Bit-exact with the reference
+ * at nbins = 8. */
+int tgvg_compute_histograms(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n,
+                            const tgvg_camera* cams, int32_t ncam, const float* const* base,
+                            const float origin[3], float r_root, int32_t nbins, uint32_t* out);
+
+/* Same, for callers that already hold the pyramids (std::vector<DepthMipmap>):
+ * levels[c] = map c's levels concatenated (host). */
+int tgvg_compute_histograms_pyr(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n,
+                                const tgvg_camera* cams, int32_t ncam,
+                                const float* const* levels, const float origin[3],
+                                float r_root, int32_t nbins, uint32_t* out);
+
+/* Device-resident form: d_cubes, d_levels (all maps' pyramids back to back,
+ * map c at element offset level_offset[c], host array) and d_out are device
+ * pointers; runs on the context stream. */
+int tgvg_compute_histograms_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, int64_t n,
+                                const tgvg_camera* cams, int32_t ncam, const float* d_levels,
+                                const int64_t* level_offset, const float origin[3],
+                                float r_root, int32_t nbins, uint32_t* d_out);
+
+/* compute_histograms_oc (reference src/histogram.hpp:55-61, histogram.cpp:222-256):
+ * cubes from a TGV1 file, leaves from the caller, output written as a TGVH file
+ * (8 bins).  The whole cube file is processed in one device pass. */
+int tgvg_compute_histograms_oc(tgvg_ctx* ctx, const char* cube_path, const tgvg_leaf* leaves,
+                               int32_t nleaf, const tgvg_camera* cams, int32_t ncam,
+                               const float* const* base, const float origin[3], float r_root,
+                               const char* out_hist_path);
+
+/* ---- Stage 6: TGV ------------------------------------------------------------
+ * tgv_minimize / tgv_minimize_oc (reference src/tgv.hpp:31-48).  mode selects the
+ * semantics (TGVG_MODE_*); leaves may be null for INMEM (one leaf covering all
+ * cubes is implied).  hists: n * nbins uint32 (host).  u_init: n floats when
+ * params->init == TGVG_INIT_GIVEN, else null.  out: n TGVCube records (host).
+ * stats may be null. */
+int tgvg_tgv_minimize(tgvg_ctx* ctx, const tgvg_cube* cubes, const uint32_t* hists, int64_t n,
+                      int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, int32_t mode,
+                      const tgvg_params* params, const float* u_init, tgvg_state* out,
+                      tgvg_stats* stats);
+
+/* Device-resident form: every array pointer is a device pointer (leaves stays
+ * on the host).  Runs on the context stream; returns after the solve finished. */
+int tgvg_tgv_minimize_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists,
+                          int64_t n, int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf,
+                          int32_t mode, const tgvg_params* params, const float* d_u_init,
+                          tgvg_state* d_out, tgvg_stats* stats);
+
+/* tgv_minimize_streaming (reference src/tgv.hpp:57-64, tgv.cpp:802-1070): TGV1
+ * cube file, TGVH histogram file (8 bins) and TGVT treetop file in, TGVS state
+ * file out.  All leaves of a level run batched in one pass on the device; the
+ * result equals the reference's leaf-by-leaf order because its leaves only see
+ * one another through the level-start snapshot. */
+int tgvg_tgv_minimize_streaming(tgvg_ctx* ctx, const char* cube_path, const char* hist_path,
+                                const char* treetop_path, const char* out_state_path,
+                                const tgvg_params* params, tgvg_stats* stats);
+
+/* ---- state / histogram files (reference tgv.cpp:24-46, histogram.cpp:175-218) */
+int tgvg_save_tgv(const char* path, const tgvg_state* state, int64_t n);
+/* Returns the record count (>= 0) and fills `out` when non-null (capacity cap). */
+int64_t tgvg_load_tgv(const char* path, tgvg_state* out, int64_t cap);
+int tgvg_save_histograms(const char* path, const uint32_t* hists, int64_t n);
+int64_t tgvg_load_histograms(const char* path, uint32_t* out, int64_t cap);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* TGVG_H */

@@ -1,0 +1,338 @@
+"""ctypes access to the oracle libraries.
+
+TEST INFRASTRUCTURE ONLY.  ``liboracle`` is the CPU restatement of the
+reference's histogram and TGV algorithms (oracle/tgv_oracle.cpp); ``libref`` is
+the reference's own src/*.cpp compiled unmodified with the project-written
+Eigen/TBB shims (oracle/Makefile, built only where the reference checkout
+exists).  Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module, as the checker or the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+from tgvreconclaude_gb300.formats import (  # noqa: E402
+    CUBE_DTYPE, LEAF_DTYPE, STATE_DTYPE, cube_keys)
+
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref.so")
+REF_DIR = os.environ.get("TGV_REFERENCE_DIR", "/root/reference")
+
+
+def build(ref: bool = False) -> None:
+    """Compile the oracle (and, when asked and the reference exists, libref)."""
+    targets = ["all"]
+    if ref and os.path.isdir(os.path.join(REF_DIR, "src")):
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", HERE, f"REF_DIR={REF_DIR}", f"-j{os.cpu_count() or 4}"]
+                   + targets, check=True)
+
+
+class Camera(C.Structure):
+    """orc::Camera: pyramid + Rt_inv (row-major) + base intrinsics."""
+    _fields_ = [("rt_inv", C.c_float * 16), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float), ("width", C.c_int32),
+                ("height", C.c_int32), ("lidar", C.c_int32), ("n_levels", C.c_int32),
+                ("dims", C.c_int32 * 26), ("offs", C.c_int64 * 13),
+                ("texels", C.POINTER(C.c_float))]
+
+
+class Params(C.Structure):
+    _fields_ = [("alpha0", C.c_float), ("alpha1", C.c_float), ("iters", C.c_int32),
+                ("init", C.c_int32), ("tol", C.c_float), ("check_every", C.c_int32)]
+
+
+class LevelStats(C.Structure):
+    _fields_ = [("depth", C.c_int32), ("iters_run", C.c_int32), ("active", C.c_int64),
+                ("residual", C.c_double), ("energy", C.c_double)]
+
+
+class RefDepthMap(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("rt", C.c_float * 16), ("width", C.c_int32), ("height", C.c_int32),
+                ("lidar", C.c_int32), ("depths", C.POINTER(C.c_float))]
+
+
+def _ptr(a, t=C.c_void_p):
+    return a.ctypes.data_as(t) if a is not None and a.size else None
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        _lib = C.CDLL(ORACLE_SO)
+        _lib.orc_median_indicator.restype = C.c_float
+        _lib.orc_mean_indicator.restype = C.c_float
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO) or os.path.isdir(os.path.join(REF_DIR, "src"))
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            build(ref=True)
+        _ref = C.CDLL(REF_SO)
+        _ref.ref_mipmap_build.restype = C.c_int64
+        _ref.ref_median_indicator.restype = C.c_float
+        _ref.ref_mean_indicator.restype = C.c_float
+    return _ref
+
+
+# ---------------------------------------------------------------- pyramids ---
+
+def pyramid_dims(w: int, h: int):
+    dims = (C.c_int32 * 26)()
+    n = lib().orc_pyramid_dims(w, h, dims)
+    return [(dims[2 * i], dims[2 * i + 1]) for i in range(n)]
+
+
+def pyramid(depth: np.ndarray):
+    """Oracle pyramid of one map -> (texels concatenated, [(w, h)...])."""
+    h, w = depth.shape
+    dims = pyramid_dims(w, h)
+    total = sum(a * b for a, b in dims)
+    out = np.empty(total, np.float32)
+    nl = C.c_int32()
+    d = (C.c_int32 * 26)()
+    base = np.ascontiguousarray(depth, np.float32)
+    lib().orc_pyramid_build(_ptr(base), w, h, _ptr(out), C.byref(nl), d)
+    return out, dims
+
+
+def make_cameras(maps):
+    """maps: list of dicts with depth (HxW f32), rt_inv (4x4), fx, fy, cx, cy, lidar.
+    Returns (ctypes Camera array, keepalive list)."""
+    cams = (Camera * max(1, len(maps)))()
+    keep = []
+    for c, m in zip(cams, maps):
+        tex, dims = pyramid(m["depth"])
+        keep.append(tex)
+        c.rt_inv[:] = [float(x) for x in np.asarray(m["rt_inv"], np.float32).reshape(16)]
+        c.fx, c.fy, c.cx, c.cy = m["fx"], m["fy"], m["cx"], m["cy"]
+        c.width, c.height = dims[0]
+        c.lidar = int(bool(m.get("lidar", False)))
+        c.n_levels = len(dims)
+        off = 0
+        for i, (a, b) in enumerate(dims):
+            c.dims[2 * i], c.dims[2 * i + 1] = a, b
+            c.offs[i] = off
+            off += a * b
+        c.texels = tex.ctypes.data_as(C.POINTER(C.c_float))
+    return cams, keep
+
+
+def compute_histograms(cubes, maps, origin, r_root, nbins=8, nthreads=1):
+    cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    cams, keep = make_cameras(maps)
+    out = np.zeros((len(cubes), nbins), np.uint32)
+    o = np.asarray(origin, np.float32)
+    rc = lib().orc_compute_histograms(_ptr(cubes), C.c_int64(len(cubes)), cams, len(maps),
+                                      _ptr(o), C.c_float(r_root), nbins, _ptr(out), nthreads)
+    assert rc == 0
+    del keep
+    return out
+
+
+def project(m, p, r_c):
+    cams, keep = make_cameras([m])
+    lv, u, v, z = C.c_int32(), C.c_int32(), C.c_int32(), C.c_float()
+    ok = lib().orc_project(cams, C.c_float(p[0]), C.c_float(p[1]), C.c_float(p[2]),
+                           C.c_float(r_c), C.byref(lv), C.byref(u), C.byref(v), C.byref(z))
+    del keep
+    return bool(ok), lv.value, u.value, v.value, z.value
+
+
+def median_indicator(bins):
+    b = np.ascontiguousarray(bins, np.uint32)
+    return lib().orc_median_indicator(_ptr(b), len(b))
+
+
+def mean_indicator(bins):
+    b = np.ascontiguousarray(bins, np.uint32)
+    return lib().orc_mean_indicator(_ptr(b), len(b))
+
+
+# ---------------------------------------------------------------------- TGV ---
+
+MODES = {"inmem": 0, "oc": 1, "stream": 2}
+INITS = {"median": 0, "zero": 1, "given": 2}
+
+
+def tgv_solve(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04, iters=200,
+              init="median", u_init=None, tol=0.0, check_every=10, fp64=False, nthreads=1):
+    """Oracle solve.  Returns (state, level_stats).  State is a STATE_DTYPE array
+    (float) or an (n, 13) float64 array when fp64."""
+    cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    hists = np.ascontiguousarray(hists, np.uint32)
+    n = len(cubes)
+    nbins = hists.shape[1] if n else 8
+    if leaves is None:
+        leaves = np.zeros(1, LEAF_DTYPE)
+        leaves["first_idx"] = 0
+        leaves["last_idx"] = max(n - 1, 0)
+        if n == 0:
+            leaves = np.zeros(0, LEAF_DTYPE)
+    leaves = np.ascontiguousarray(leaves, LEAF_DTYPE)
+    p = Params(alpha0, alpha1, iters, INITS[init], tol, check_every)
+    ui = None if u_init is None else np.ascontiguousarray(u_init, np.float32)
+    ls = (LevelStats * 24)()
+    nls = C.c_int()
+    if fp64:
+        out = np.zeros((n, 13), np.float64)
+        fn = lib().orc_tgv_solve_f64
+    else:
+        out = np.zeros(n, STATE_DTYPE)
+        fn = lib().orc_tgv_solve
+    rc = fn(_ptr(cubes), _ptr(hists), C.c_int64(n), nbins, _ptr(leaves), len(leaves),
+            MODES[mode], C.byref(p), _ptr(ui), _ptr(out), ls, C.byref(nls), nthreads)
+    assert rc == 0, rc
+    stats = [dict(depth=ls[i].depth, iters_run=ls[i].iters_run, active=ls[i].active,
+                  residual=ls[i].residual) for i in range(nls.value)]
+    return out, stats
+
+
+# ------------------------------------------------------ reference (libref) ---
+
+def _refmap(m):
+    d = RefDepthMap()
+    d.fx, d.fy, d.cx, d.cy = m["fx"], m["fy"], m["cx"], m["cy"]
+    d.rt[:] = [float(x) for x in np.asarray(m["rt"], np.float32).reshape(16)]
+    h, w = m["depth"].shape
+    d.width, d.height = w, h
+    d.lidar = int(bool(m.get("lidar", False)))
+    arr = np.ascontiguousarray(m["depth"], np.float32)
+    d.depths = arr.ctypes.data_as(C.POINTER(C.c_float))
+    return d, arr
+
+
+def ref_mipmap(m):
+    """Reference DepthMipmap::build -> (rt_inv 4x4, texels, dims)."""
+    d, keep = _refmap(m)
+    rt_inv = np.zeros(16, np.float32)
+    nl = C.c_int32()
+    dims = (C.c_int32 * 26)()
+    total = ref().ref_mipmap_build(C.byref(d), _ptr(rt_inv), C.byref(nl), dims, None)
+    tex = np.zeros(total, np.float32)
+    ref().ref_mipmap_build(C.byref(d), _ptr(rt_inv), C.byref(nl), dims, _ptr(tex))
+    del keep
+    return rt_inv.reshape(4, 4), tex, [(dims[2 * i], dims[2 * i + 1]) for i in range(nl.value)]
+
+
+def ref_compute_histograms(cubes, maps, origin, r_root):
+    cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    arr = (RefDepthMap * max(1, len(maps)))()
+    keep = []
+    for i, m in enumerate(maps):
+        d, k = _refmap(m)
+        arr[i] = d
+        keep.append(k)
+    out = np.zeros((len(cubes), 8), np.uint32)
+    rc = ref().ref_compute_histograms(_ptr(cubes), C.c_int64(len(cubes)), arr, len(maps),
+                                      C.c_float(origin[0]), C.c_float(origin[1]),
+                                      C.c_float(origin[2]), C.c_float(r_root), _ptr(out))
+    assert rc == 0
+    return out
+
+
+def ref_project(m, p, r_c):
+    d, keep = _refmap(m)
+    lv, u, v, z = C.c_int32(), C.c_int32(), C.c_int32(), C.c_float()
+    ok = ref().ref_project(C.byref(d), C.c_float(p[0]), C.c_float(p[1]), C.c_float(p[2]),
+                           C.c_float(r_c), C.byref(lv), C.byref(u), C.byref(v), C.byref(z))
+    return bool(ok), lv.value, u.value, v.value, z.value
+
+
+def ref_median_indicator(bins8):
+    b = np.ascontiguousarray(bins8, np.uint32)
+    return ref().ref_median_indicator(_ptr(b))
+
+
+def ref_mean_indicator(bins8):
+    b = np.ascontiguousarray(bins8, np.uint32)
+    return ref().ref_mean_indicator(_ptr(b))
+
+
+def ref_tgv(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04, iters=200,
+            r_root=1.0, tmpdir=None):
+    """The reference's tgv_minimize / tgv_minimize_oc / tgv_minimize_streaming."""
+    import tempfile
+    from tgvreconclaude_gb300 import formats
+    cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    hists = np.ascontiguousarray(hists, np.uint32)
+    assert hists.shape[1] == 8
+    n = len(cubes)
+    out = np.zeros(n, STATE_DTYPE)
+    if mode == "inmem":
+        rc = ref().ref_tgv_minimize(_ptr(cubes), _ptr(hists), C.c_int64(n), C.c_float(alpha0),
+                                    C.c_float(alpha1), iters, C.c_float(r_root), _ptr(out))
+        assert rc == 0
+        return out
+    leaves = np.ascontiguousarray(leaves, LEAF_DTYPE)
+    if mode == "oc":
+        rc = ref().ref_tgv_minimize_oc(_ptr(cubes), _ptr(hists), C.c_int64(n), _ptr(leaves),
+                                       len(leaves), C.c_float(alpha0), C.c_float(alpha1), iters,
+                                       C.c_float(r_root), _ptr(out))
+        assert rc == 0
+        return out
+    with tempfile.TemporaryDirectory(dir=tmpdir) as td:
+        cp, hp, tp, sp = (os.path.join(td, x) for x in ("c.bin", "h.bin", "t.bin", "s.bin"))
+        formats.save_cubes(cp, cubes, r_root)
+        formats.save_histograms(hp, hists)
+        formats.save_treetop(tp, leaves, r_root)
+        rc = ref().ref_tgv_minimize_streaming(cp.encode(), hp.encode(), tp.encode(),
+                                              C.c_float(r_root), sp.encode(), C.c_float(alpha0),
+                                              C.c_float(alpha1), iters)
+        assert rc == 0
+        return formats.load_state(sp)
+
+
+def ref_pipeline_cubes(maps, origin, r_root, tmpdir=None):
+    """Reference Stages 1-4 on base depth maps (fixture generation only):
+    build_cubes_from_depthmap per map, kway_merge, balance_octree, build_treetop.
+    Returns (balanced cubes, treetop leaves)."""
+    import tempfile
+    from tgvreconclaude_gb300 import formats
+    with tempfile.TemporaryDirectory(dir=tmpdir) as td:
+        paths = []
+        for i, m in enumerate(maps):
+            d, keep = _refmap(m)
+            p = os.path.join(td, f"m{i}.cubes")
+            rc = ref().ref_build_cubes_from_depthmap(C.byref(d), C.c_float(origin[0]),
+                                                     C.c_float(origin[1]), C.c_float(origin[2]),
+                                                     C.c_float(r_root), p.encode())
+            assert rc == 0
+            paths.append(p)
+        arr = (C.c_char_p * len(paths))(*[p.encode() for p in paths])
+        merged, bal, tt = (os.path.join(td, x) for x in ("m.cubes", "b.cubes", "t.bin"))
+        assert ref().ref_kway_merge(arr, len(paths), merged.encode()) == 0
+        assert ref().ref_balance_octree(merged.encode(), bal.encode()) == 0
+        assert ref().ref_build_treetop(bal.encode(), tt.encode()) == 0
+        cubes, _ = formats.load_cubes(bal)
+        leaves, _ = formats.load_treetop(tt)
+        return cubes, leaves
+
+
+__all__ = ["build", "lib", "ref", "ref_available", "compute_histograms", "pyramid",
+           "pyramid_dims", "project", "median_indicator", "mean_indicator", "tgv_solve",
+           "ref_mipmap", "ref_compute_histograms", "ref_project", "ref_median_indicator",
+           "ref_mean_indicator", "ref_tgv", "ref_pipeline_cubes", "cube_keys"]

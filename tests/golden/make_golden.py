@@ -1,0 +1,104 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs the reference's own src/histogram.cpp and src/tgv.cpp (compiled unmodified
+into oracle/_ref/libref.so by oracle/Makefile, with the project-written
+Eigen/TBB shims) on seeded synthetic inputs and stores inputs + outputs as
+compressed .npz files.  Needs the reference checkout (TGV_REFERENCE_DIR,
+default /root/reference); the fixtures it writes are committed so the tests can
+run where the reference is absent.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+import oracle as O  # noqa: E402
+from tgvreconclaude_gb300 import formats as F, scenes as S  # noqa: E402
+
+
+def maps_for(scene, rig, seed0=0, lidar_every=0):
+    maps = []
+    for i, c in enumerate(rig):
+        d = S.render_depth(scene, c, seed=seed0 + i).numpy()
+        m = dict(depth=d, rt=c["rt"], fx=c["fx"], fy=c["fy"], cx=c["cx"], cy=c["cy"],
+                 lidar=bool(lidar_every and i % lidar_every == 0))
+        m["rt_inv"], _, _ = O.ref_mipmap(m)
+        maps.append(m)
+    return maps
+
+
+def pack_maps(maps):
+    return dict(depths=np.stack([m["depth"] for m in maps]), rt=np.stack([m["rt"] for m in maps]),
+                rt_inv=np.stack([m["rt_inv"] for m in maps]),
+                k=np.array([[m["fx"], m["fy"], m["cx"], m["cy"]] for m in maps], np.float32),
+                lidar=np.array([m["lidar"] for m in maps], bool))
+
+
+def hist_case(name, rng, scene, rig, cubes, origin, r_root, lidar_every=0):
+    maps = maps_for(scene, rig, int(rng.integers(1 << 30)), lidar_every)
+    bins = O.ref_compute_histograms(cubes, maps, origin, r_root)
+    np.savez_compressed(os.path.join(HERE, f"hist_{name}.npz"), cubes=cubes, origin=np.float32(origin),
+                        r_root=np.float32(r_root), bins=bins, **pack_maps(maps))
+    print(f"hist_{name}: {len(cubes)} cubes, {len(maps)} maps, votes {int(bins.sum())}")
+
+
+def tgv_case(name, cubes, hists, leaves, alpha0, alpha1, iters, r_root=1.0):
+    out = {}
+    for mode in ("inmem", "oc", "stream"):
+        out[mode] = O.ref_tgv(cubes, hists, leaves, mode, alpha0, alpha1, iters, r_root=r_root)
+    np.savez_compressed(os.path.join(HERE, f"tgv_{name}.npz"), cubes=cubes, hists=hists, leaves=leaves,
+                        params=np.array([alpha0, alpha1], np.float32), iters=np.int32(iters),
+                        inmem=out["inmem"], oc=out["oc"], stream=out["stream"])
+    d = np.bincount(cubes["depth"])
+    print(f"tgv_{name}: {len(cubes)} cubes, depths {np.nonzero(d)[0].tolist()}, leaves {len(leaves)}")
+
+
+def main():
+    O.build(ref=True)
+    rng = np.random.default_rng(20261203)
+
+    # Stage 5: torus seen by a sphere rig (one LIDAR map), cubes from a random band
+    scene = S.torus_scene(0.005)
+    rig = S.sphere_rig(6, 3.0, width=96, height=72)
+    cubes = S.random_octree(rng, dmin=3, dmax=7, target=4000, shape="sphere", r_root=1.5)
+    cubes["r_c"][:6] = [0.0, -1.0, np.nan, np.inf, 100.0, 1e-6]
+    hist_case("torus", rng, scene, rig, cubes, (-1.5, -1.5, -1.5), 1.5, lidar_every=4)
+
+    # Stage 5: three objects with the cubes of the reference's own Stages 1-4
+    scene3 = S.three_objects_scene(rng)
+    rig3 = S.sphere_rig(8, 6.0, width=80, height=60, half_fov_deg=28)
+    maps3 = maps_for(scene3, rig3, 100)
+    cubes3, leaves3 = O.ref_pipeline_cubes(maps3[:3], (-3.0, -3.0, -3.0), 3.0)
+    if len(cubes3) > 6000:
+        cubes3 = cubes3[:6000]
+    hist_case("three", rng, scene3, rig3, cubes3, (-3.0, -3.0, -3.0), 3.0)
+
+    # Stage 6: random multi-level octrees with duplicate codes, several leaf splits
+    for k, (shape, dmin, dmax, nleaf, aligned, a0, a1, it) in enumerate([
+            ("sphere", 2, 5, 3, True, 0.02, 0.04, 25),
+            ("plane", 3, 6, 4, False, 0.1, 0.2, 30),
+            ("random", 1, 4, 2, False, 1.0, 2.0, 20)]):
+        c = S.random_octree(rng, dmin=dmin, dmax=dmax, target=1500, shape=shape)
+        h = S.random_histograms(rng, len(c))
+        lv = S.split_leaves(len(c), nleaf, rng, c, aligned=aligned)
+        tgv_case(f"rand{k}", c, h, lv, a0, a1, it)
+
+    # Stage 6: reference-built balanced octree (Stages 1-4) with reference histograms
+    maps_b = maps_for(S.torus_scene(0.005), S.sphere_rig(3, 3.0, width=64, height=48), 300)
+    cb, lb = O.ref_pipeline_cubes(maps_b, (-1.5, -1.5, -1.5), 1.5)
+    hb = O.ref_compute_histograms(cb, maps_b, (-1.5, -1.5, -1.5), 1.5)
+    lv = S.split_leaves(len(cb), 3, rng, cb, aligned=True)
+    tgv_case("balanced", cb, hb, lv, 2.0, 1.0, 40, r_root=1.5)
+
+
+if __name__ == "__main__":
+    main()

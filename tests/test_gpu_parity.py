@@ -1,0 +1,270 @@
+"""GPU parity: the sm_103a path through the C ABI against the oracle and the
+reference's golden fixtures.
+
+Bars: histograms and pyramids bit-exact; TGV states bit-exact with the oracle
+(which is itself bit-exact with the reference), and always within the stated
+tolerance max|du| <= 1e-4.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_maps, load_golden
+from tgvreconclaude_gb300 import _native as N, api, formats as F, scenes as S
+
+pytestmark = pytest.mark.gpu
+TOL_U = 1e-4
+
+TGV_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "tgv_*.npz")))
+HIST_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "hist_*.npz")))
+
+
+def cams_from(maps):
+    out = []
+    for m in maps:
+        c = N.Camera()
+        c.rt_inv[:] = [float(v) for v in np.asarray(m["rt_inv"], np.float32).reshape(16)]
+        c.fx, c.fy, c.cx, c.cy = m["fx"], m["fy"], m["cx"], m["cy"]
+        h, w = m["depth"].shape
+        c.width, c.height = w, h
+        c.lidar = int(bool(m.get("lidar", False)))
+        out.append(c)
+    return out
+
+
+def render_maps(scene, rig, seed=0, lidar_every=0):
+    maps = []
+    for i, c in enumerate(rig):
+        d = S.render_depth(scene, c, seed=seed + i).numpy()
+        rt_inv = np.linalg.inv(np.asarray(c["rt"], np.float64)).astype(np.float32)
+        maps.append(dict(depth=d, rt=c["rt"], rt_inv=rt_inv, fx=c["fx"], fy=c["fy"], cx=c["cx"], cy=c["cy"],
+                         lidar=bool(lidar_every and i % lidar_every == 0)))
+    return maps
+
+
+def assert_state_equal(gpu, ref, what=""):
+    du = np.abs(gpu["u"].astype(np.float64) - ref["u"]).max() if len(ref) else 0.0
+    assert du <= TOL_U, f"{what}: max|du| = {du}"
+    assert gpu.tobytes() == ref.tobytes(), f"{what}: not bit-identical (max|du| = {du})"
+
+
+# ------------------------------------------------------------- Stage 5 ---
+
+@pytest.mark.parametrize("case", HIST_CASES)
+def test_histograms_match_golden(case):
+    g = load_golden(case)
+    maps = golden_maps(g)
+    bins = api.compute_histograms_from_maps(g["cubes"], cams_from(maps), [m["depth"] for m in maps], g["origin"],
+                                            float(g["r_root"]))
+    assert np.array_equal(bins, g["bins"])
+
+
+def test_pyramids_bitexact(oracle_lib):
+    rng = np.random.default_rng(5)
+    for (h, w) in [(37, 50), (1, 9), (64, 2), (480, 640), (1080, 1920), (5, 5)]:
+        d = rng.uniform(0.5, 5.0, (h, w)).astype(np.float32)
+        d[rng.random((h, w)) < 0.2] = np.nan
+        d[rng.random((h, w)) < 0.05] = -1.0
+        d[rng.random((h, w)) < 0.02] = np.inf
+        d[rng.random((h, w)) < 0.02] = 0.0
+        mm = api.DepthMipmap().build(api.DepthMap(w, h, d))
+        ref, dims = oracle_lib.pyramid(d)
+        assert mm.dims == dims
+        assert mm._flat.view(np.uint32).tobytes() == ref.view(np.uint32).tobytes(), (h, w)
+
+
+@pytest.mark.parametrize("nbins", [8, 10])
+def test_histograms_random_scenes(oracle_lib, nbins):
+    rng = np.random.default_rng(11 + nbins)
+    scene = S.three_objects_scene(rng)
+    maps = render_maps(scene, S.sphere_rig(12, 6.0, width=160, height=120, half_fov_deg=28), 40, lidar_every=5)
+    cubes = S.random_octree(rng, dmin=3, dmax=9, target=60000, shape="sphere", r_root=3.0)
+    cubes["r_c"][:8] = [0.0, -2.0, np.nan, np.inf, 1e9, 1e-30, -0.0, 5.0]
+    ref = oracle_lib.compute_histograms(cubes, maps, (-3.0, -3.0, -3.0), 3.0, nbins=nbins, nthreads=8)
+    gpu = api.compute_histograms_from_maps(cubes, cams_from(maps), [m["depth"] for m in maps], (-3.0, -3.0, -3.0),
+                                           3.0, nbins=nbins)
+    assert ref.sum() > 0
+    assert np.array_equal(gpu, ref)
+
+
+def test_histograms_via_depth_mipmap(oracle_lib):
+    """The DepthMipmap route (pyramids built on the GPU, then compute_histograms)."""
+    rng = np.random.default_rng(2)
+    rig = S.sphere_rig(5, 3.0, width=120, height=90)
+    maps = render_maps(S.torus_scene(), rig, 7, lidar_every=2)
+    mms = []
+    for m in maps:
+        mm = api.DepthMipmap().build(api.DepthMap(120, 90, m["depth"], K=np.array(
+            [[m["fx"], 0, m["cx"]], [0, m["fy"], m["cy"]], [0, 0, 1]], np.float32), Rt=m["rt"]), m["lidar"])
+        m["rt_inv"] = mm.Rt_inv
+        mms.append(mm)
+    cubes = S.random_octree(rng, dmin=3, dmax=8, target=20000, r_root=1.5)
+    gpu = api.compute_histograms(cubes, mms, (-1.5, -1.5, -1.5), 1.5)
+    ref = oracle_lib.compute_histograms(cubes, maps, (-1.5, -1.5, -1.5), 1.5)
+    assert np.array_equal(gpu, ref)
+    # project / depth_at mirror the reference's per-point API (test_stage5.cpp:45-80)
+    c = F.cube_keys(cubes[:50])
+    for i in range(50):
+        x, y, z = (int(v) for v in F.morton_decode(np.uint64(c[i])))
+        d = int(cubes["depth"][i]); cs = 3.0 / (1 << d)
+        P = [-1.5 + ((v >> (21 - d)) + 0.5) * cs for v in (x, y, z)]
+        assert mms[0].project(P, float(cubes["r_c"][i]))[0] == oracle_lib.project(maps[0], P, float(cubes["r_c"][i]))[0]
+
+
+def test_histograms_empty_and_no_cameras():
+    e = api.compute_histograms_from_maps(np.zeros(0, F.CUBE_DTYPE), [], [], (0, 0, 0), 1.0)
+    assert e.shape == (0, 8)
+    rng = np.random.default_rng(0)
+    cubes = S.random_octree(rng, 2, 4, 100)
+    z = api.compute_histograms_from_maps(cubes, [], [], (0, 0, 0), 1.0)
+    assert z.shape == (len(cubes), 8) and z.sum() == 0
+
+
+def test_histograms_oc_file(tmp_path, oracle_lib):
+    """compute_histograms_oc: cube file + leaves in, TGVH out (histogram.cpp:222-256)."""
+    g = load_golden("hist_torus.npz")
+    maps = golden_maps(g)
+    cp, hp = tmp_path / "c.bin", tmp_path / "h.bin"
+    F.save_cubes(cp, g["cubes"], float(g["r_root"]))
+    leaves = S.split_leaves(len(g["cubes"]), 5, np.random.default_rng(1), g["cubes"])
+    mms = []
+    for m in maps:
+        mm = api.DepthMipmap().build(api.DepthMap(m["depth"].shape[1], m["depth"].shape[0], m["depth"], K=np.array(
+            [[m["fx"], 0, m["cx"]], [0, m["fy"], m["cy"]], [0, 0, 1]], np.float32), Rt=m["rt"]), m["lidar"])
+        mm.Rt_inv = m["rt_inv"]
+        mms.append(mm)
+    api.compute_histograms_oc(cp, leaves, mms, g["origin"], float(g["r_root"]), hp)
+    assert np.array_equal(F.load_histograms(hp), g["bins"])
+
+
+# ------------------------------------------------------------- Stage 6 ---
+
+@pytest.mark.parametrize("case", TGV_CASES)
+@pytest.mark.parametrize("mode", ["inmem", "oc", "stream"])
+def test_tgv_matches_golden(case, mode):
+    g = load_golden(case)
+    a0, a1 = (float(x) for x in g["params"])
+    prm = api.TGVParams(alpha0=a0, alpha1=a1, iters=int(g["iters"]))
+    out, st = api.tgv_solve(g["cubes"], g["hists"], g["leaves"], mode, prm)
+    assert_state_equal(out, g[mode], f"{case}/{mode}")
+    assert st["leaf_iters"] == len(g["cubes"]) * int(g["iters"])  # golden leaves cover every cube
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_tgv_random_vs_oracle(oracle_lib, seed):
+    rng = np.random.default_rng(500 + seed)
+    nbins = 10 if seed % 3 == 2 else 8
+    cubes = S.random_octree(rng, dmin=seed % 3, dmax=3 + seed % 4, target=3000 + 2000 * seed,
+                            shape=["sphere", "plane", "random"][seed % 3])
+    hists = S.random_histograms(rng, len(cubes), nbins=nbins)
+    leaves = S.split_leaves(len(cubes), 1 + 2 * seed, rng, cubes, aligned=seed % 2 == 0)
+    init = ["median", "zero", "given"][seed % 3]
+    u0 = rng.uniform(-1, 1, len(cubes)).astype(np.float32) if init == "given" else None
+    for mode in ("inmem", "oc", "stream"):
+        a0, a1 = [(0.02, 0.04), (2.0, 1.0), (0.3, 0.1)][seed % 3]
+        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, a0, a1, 17, init=init, u_init=u0)
+        out, _ = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(a0, a1, 17, init=init), u_init=u0)
+        assert_state_equal(out, ref, f"seed {seed} {mode}")
+
+
+def test_tgv_unsorted_inmem_and_leaf_gaps(oracle_lib):
+    """In-memory semantics need no ordering; leaves may leave cubes uncovered."""
+    rng = np.random.default_rng(9)
+    cubes = S.random_octree(rng, 2, 6, 4000)
+    perm = rng.permutation(len(cubes))
+    cu, h = cubes[perm], S.random_histograms(rng, len(cubes))
+    ref, _ = oracle_lib.tgv_solve(cu, h, None, "inmem", 0.5, 0.5, 15)
+    out, _ = api.tgv_solve(cu, h, None, "inmem", api.TGVParams(0.5, 0.5, 15))
+    assert_state_equal(out, ref, "unsorted inmem")
+    leaves = S.split_leaves(len(cubes), 4, rng, cubes)
+    leaves = leaves[[0, 2, 3]]  # leaf 1's cubes are in no leaf
+    leaves = leaves[::-1].copy()  # order given by the caller
+    for mode in ("oc", "stream"):
+        ref, _ = oracle_lib.tgv_solve(cubes, h, leaves, mode, 0.5, 0.5, 15)
+        out, _ = api.tgv_solve(cubes, h, leaves, mode, api.TGVParams(0.5, 0.5, 15))
+        assert_state_equal(out, ref, f"gaps {mode}")
+
+
+def test_tgv_stopping_rule(oracle_lib):
+    """Per-level (per-leaf in streaming) stop at relative residual <= tol.  A
+    level that stops early has residual <= tol; the iteration counts and the
+    final state agree with the oracle.  (Cubes without votes make the
+    reference's iteration drift, so some levels may run to the cap.)"""
+    rng = np.random.default_rng(4)
+    cubes = S.random_octree(rng, 2, 6, 8000)
+    h = S.random_histograms(rng, len(cubes), empty_frac=0.0)
+    h[h.sum(1) == 0, 3] = 1
+    leaves = S.split_leaves(len(cubes), 3, rng, cubes, aligned=True)
+    for mode in ("inmem", "stream"):
+        ref, rst = oracle_lib.tgv_solve(cubes, h, leaves, mode, 1.0, 2.0, 1500, tol=1e-4, check_every=10)
+        out, st = api.tgv_solve(cubes, h, leaves, mode, api.TGVParams(1.0, 2.0, 1500, tol=1e-4, check_every=10))
+        assert [r["iters_run"] for r in rst] == st["iters_run"], mode
+        assert any(i < 1500 for i in st["iters_run"])
+        assert all(r <= 1e-4 for r, i in zip(st["residual"], st["iters_run"]) if i < 1500)
+        assert_state_equal(out, ref, f"stop {mode}")
+
+
+def test_tgv_reference_kats():
+    """tests/test_stage6.cpp:25-184 through the GPU API."""
+    cubes = F.make_cubes([int(F.morton_encode(np.uint32(ix << 16), np.uint32(0), np.uint32(0))) for ix in range(3)],
+                         5, 1.0)
+    h = np.zeros((3, 8), np.uint32); h[0, 6] = 50; h[2, 1] = 50
+    p = api.TGVParams(alpha0=0.1, alpha1=0.2, iters=50)
+    s = api.tgv_minimize(cubes, h, None, 32.0, p)
+    assert s["u"][0] > 0 > s["u"][2] and s["u"][2] < s["u"][1] < s["u"][0]
+    one = np.zeros(1, F.LEAF_DTYPE); one["last_idx"] = 2
+    two = np.zeros(2, F.LEAF_DTYPE); two["first_idx"] = [0, 2]; two["last_idx"] = [1, 2]
+    assert np.abs(api.tgv_minimize_oc(cubes, h, one, None, 32.0, p)["u"] - s["u"]).max() <= 1e-5
+    s2 = api.tgv_minimize_oc(cubes, h, two, None, 32.0, p)
+    assert s2["u"][0] > 0 > s2["u"][2] and s2["u"][2] < s2["u"][1] < s2["u"][0]
+    c4 = F.make_cubes([int(F.morton_encode(np.uint32(ix << 17), np.uint32(0), np.uint32(0))) for ix in range(4)], 4, 1.0)
+    h4 = np.zeros((4, 8), np.uint32); h4[:, 6] = 10
+    s4 = api.tgv_minimize(c4, h4, None, 16.0, api.TGVParams(iters=20))
+    assert np.all(np.abs(s4["u"] - 0.625) <= 0.15)
+    assert len(api.tgv_minimize_oc(np.zeros(0, F.CUBE_DTYPE), np.zeros((0, 8), np.uint32),
+                                   np.zeros(0, F.LEAF_DTYPE), None, 1.0)) == 0
+
+
+def test_tgv_streaming_files(tmp_path):
+    """tgv_minimize_streaming: TGV1/TGVH/TGVT in, TGVS out (test_stage6.cpp:242-344)."""
+    g = load_golden("tgv_balanced.npz")
+    cp, hp, tp, sp = (tmp_path / x for x in ("c", "h", "t", "s"))
+    F.save_cubes(cp, g["cubes"], 1.5)
+    F.save_histograms(hp, g["hists"])
+    F.save_treetop(tp, g["leaves"], 1.5)
+    a0, a1 = (float(x) for x in g["params"])
+    api.tgv_minimize_streaming(cp, hp, tp, None, 1.5, sp, api.TGVParams(a0, a1, int(g["iters"])))
+    assert_state_equal(F.load_state(sp), g["stream"], "streaming files")
+    F.save_cubes(cp, np.zeros(0, F.CUBE_DTYPE), 1.5)
+    api.tgv_minimize_streaming(cp, hp, tp, None, 1.5, sp)
+    assert len(F.load_state(sp)) == 0
+
+
+def test_tgv_errors(tmp_path):
+    rng = np.random.default_rng(1)
+    cubes = S.random_octree(rng, 2, 5, 500)
+    h = S.random_histograms(rng, len(cubes))
+    lv = S.split_leaves(len(cubes), 2, rng, cubes)
+    with pytest.raises(RuntimeError, match="sorted"):
+        api.tgv_solve(cubes[::-1].copy(), h, lv, "stream")
+    bad = lv.copy(); bad["last_idx"][0] = bad["first_idx"][1] + 3
+    with pytest.raises(RuntimeError, match="overlap"):
+        api.tgv_solve(cubes, h, bad, "oc")
+    dbad = cubes.copy(); dbad["depth"][3] = 22
+    with pytest.raises(RuntimeError, match="invalid"):
+        api.tgv_solve(dbad, h, None, "inmem")
+    (tmp_path / "x").write_bytes(b"XXXX" + bytes(20))
+    with pytest.raises(RuntimeError, match="magic"):
+        api.tgv_minimize_streaming(tmp_path / "x", tmp_path / "x", tmp_path / "x", None, 1.0, tmp_path / "o")
+
+
+def test_constant_field_is_a_fixed_point():
+    """Size-independent property: identical histograms everywhere -> u stays at
+    the common median exactly and v, p, q stay 0, at any size."""
+    rng = np.random.default_rng(3)
+    cubes = S.random_octree(rng, 3, 7, 400000)
+    h = np.zeros((len(cubes), 8), np.uint32); h[:, 5] = 7
+    out, st = api.tgv_solve(cubes, h, None, "inmem", api.TGVParams(1.0, 2.0, 30))
+    assert np.all(out["u"] == np.float32(0.375)) and not out["v"].any() and not out["p"].any() and not out["q"].any()

@@ -1,0 +1,183 @@
+"""The oracle (oracle/tgv_oracle.cpp) against the reference's own outputs.
+
+CPU only.  Pins the restatement bit for bit: against the committed golden
+fixtures (made by the unmodified reference, tests/golden/make_golden.py) and,
+where the reference checkout exists, against the reference compiled here on
+fresh seeded inputs.  Also restates the reference's own known-answer tests
+(tests/test_stage5.cpp, tests/test_stage6.cpp) against the oracle.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_maps, load_golden
+from tgvreconclaude_gb300 import formats as F, scenes as S
+
+TGV_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "tgv_*.npz")))
+HIST_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "hist_*.npz")))
+
+
+@pytest.mark.parametrize("case", TGV_CASES)
+@pytest.mark.parametrize("mode", ["inmem", "oc", "stream"])
+def test_oracle_tgv_matches_golden(oracle_lib, case, mode):
+    g = load_golden(case)
+    a0, a1 = (float(x) for x in g["params"])
+    out, _ = oracle_lib.tgv_solve(g["cubes"], g["hists"], g["leaves"], mode, a0, a1, int(g["iters"]))
+    assert out.tobytes() == g[mode].tobytes()
+
+
+@pytest.mark.parametrize("case", HIST_CASES)
+def test_oracle_histograms_match_golden(oracle_lib, case):
+    g = load_golden(case)
+    bins = oracle_lib.compute_histograms(g["cubes"], golden_maps(g), g["origin"], float(g["r_root"]))
+    assert np.array_equal(bins, g["bins"])
+
+
+def test_level_thresholds_exhaustive(oracle_lib):
+    """The product's pyramid-level thresholds give (int)log2f(x) for every float
+    x in [1, 2^14) (and at the top of the range) on this host."""
+    import ctypes as C
+    from tgvreconclaude_gb300 import _native as N
+    t = (C.c_float * 13)()
+    N.lib().tgvg_level_thresholds(t)
+    arr = np.array(t[:], np.float32)
+    assert arr[0] == 1.0 and np.all(np.diff(arr) > 0)
+    assert arr[1] <= 2.0 and arr[12] <= 4096.0
+    oracle_lib.lib().orc_check_thresholds.restype = C.c_int64
+    assert oracle_lib.lib().orc_check_thresholds(t) == 0
+
+
+# --------------------------------------------------------- live reference ---
+
+needs_ref = pytest.mark.skipif(not __import__("oracle").ref_available(), reason="reference checkout absent")
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", range(4))
+def test_oracle_tgv_matches_reference(oracle_lib, seed):
+    rng = np.random.default_rng(1000 + seed)
+    cubes = S.random_octree(rng, dmin=1 + seed % 3, dmax=4 + seed % 3, target=900,
+                            shape=["sphere", "plane", "random"][seed % 3])
+    hists = S.random_histograms(rng, len(cubes))
+    leaves = S.split_leaves(len(cubes), 2 + seed, rng, cubes, aligned=bool(seed % 2))
+    for mode in ("inmem", "oc", "stream"):
+        ref = oracle_lib.ref_tgv(cubes, hists, leaves, mode, 0.05 * (seed + 1), 0.1 * (seed + 1), 12)
+        out, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 0.05 * (seed + 1), 0.1 * (seed + 1), 12)
+        assert out.tobytes() == ref.tobytes(), mode
+
+
+@needs_ref
+def test_oracle_histograms_and_pyramids_match_reference(oracle_lib):
+    rng = np.random.default_rng(7)
+    rig = S.sphere_rig(4, 3.0, width=50, height=37)  # odd sizes exercise the pyramid edges
+    maps = []
+    for i, c in enumerate(rig):
+        d = S.render_depth(S.torus_scene(0.01), c, seed=i).numpy()
+        d[::7, ::5] = np.nan
+        d[3, :] = -1.0
+        m = dict(depth=d, rt=c["rt"], fx=c["fx"], fy=c["fy"], cx=c["cx"], cy=c["cy"], lidar=i == 1)
+        m["rt_inv"], tex, dims = oracle_lib.ref_mipmap(m)
+        otex, odims = oracle_lib.pyramid(d)
+        assert dims == odims
+        assert tex.view(np.uint32).tobytes() == otex.view(np.uint32).tobytes()
+        maps.append(m)
+    cubes = S.random_octree(rng, dmin=2, dmax=8, target=3000, r_root=1.5)
+    for nb in (8,):
+        ref = oracle_lib.ref_compute_histograms(cubes, maps, (-1.5, -1.5, -1.5), 1.5)
+        out = oracle_lib.compute_histograms(cubes, maps, (-1.5, -1.5, -1.5), 1.5, nbins=nb)
+        assert np.array_equal(ref, out)
+
+
+@needs_ref
+def test_morton_helpers_match_reference(oracle_lib):
+    import ctypes as C
+    rng = np.random.default_rng(3)
+    r = oracle_lib.ref()
+    for _ in range(300):
+        d = int(rng.integers(1, 22))
+        x, y, z = (int(v) << (21 - d) for v in rng.integers(0, 1 << d, 3))
+        k = int(F.morton_encode(np.uint32(x), np.uint32(y), np.uint32(z)))
+        hi, lo = k >> 32, k & 0xffffffff
+        oh, ol = C.c_uint32(), C.c_uint32()
+        r.ref_parent_code(C.c_uint32(hi), C.c_uint32(lo), d, C.byref(oh), C.byref(ol))
+        assert (oh.value << 32 | ol.value) == int(F.ancestor_key(np.uint64(k), d - 1))
+        for f in range(6):
+            r.ref_face_neighbor(C.c_uint32(hi), C.c_uint32(lo), f, d, C.byref(oh), C.byref(ol))
+            step = 1 << (21 - d)
+            c = [x, y, z]
+            ax, sgn = f // 2, 1 if f % 2 == 0 else -1
+            c[ax] += sgn * step
+            if c[ax] < 0 or c[ax] >= 1 << 21:
+                assert (oh.value, ol.value) == (0xffffffff, 0xffffffff)
+            else:
+                kk = int(F.morton_encode(np.uint32(c[0]), np.uint32(c[1]), np.uint32(c[2])))
+                assert (oh.value << 32 | ol.value) == kk
+
+
+# ------------------------------------- the reference's known-answer tests ---
+
+def _chain(r_root=32.0):
+    cubes = F.make_cubes([int(F.morton_encode(np.uint32(ix << 16), np.uint32(0), np.uint32(0))) for ix in range(3)],
+                         5, r_root / 32)
+    h = np.zeros((3, 8), np.uint32)
+    h[0, 6] = 50
+    h[2, 1] = 50
+    return cubes, h
+
+
+def test_kat_stage6_smoothing_and_chunks(oracle_lib):
+    """tests/test_stage6.cpp:25-66, 133-175, 242-310: polarity and B between A and C."""
+    cubes, h = _chain()
+    one = np.zeros(1, F.LEAF_DTYPE); one["last_idx"] = 2
+    two = np.zeros(2, F.LEAF_DTYPE); two["last_idx"] = [1, 2]; two["first_idx"] = [0, 2]
+    s1, _ = oracle_lib.tgv_solve(cubes, h, None, "inmem", 0.1, 0.2, 50)
+    for st in (s1,) + tuple(oracle_lib.tgv_solve(cubes, h, lv, m, 0.1, 0.2, 50)[0]
+                            for m in ("oc", "stream") for lv in (one, two)):
+        assert st["u"][0] > 0 and st["u"][2] < 0 and st["u"][2] < st["u"][1] < st["u"][0]
+    so, _ = oracle_lib.tgv_solve(cubes, h, one, "oc", 0.1, 0.2, 50)
+    ss, _ = oracle_lib.tgv_solve(cubes, h, one, "stream", 0.1, 0.2, 50)
+    assert np.abs(so["u"] - s1["u"]).max() <= 1e-5
+    assert np.abs(ss["u"] - s1["u"]).max() <= 1e-4
+
+
+def test_kat_stage6_constant_and_empty(oracle_lib):
+    """tests/test_stage6.cpp:68-94 and 178-184."""
+    cubes = F.make_cubes([int(F.morton_encode(np.uint32(ix << 17), np.uint32(0), np.uint32(0))) for ix in range(4)],
+                         4, 1.0)
+    h = np.zeros((4, 8), np.uint32); h[:, 6] = 10
+    st, _ = oracle_lib.tgv_solve(cubes, h, None, "inmem", 0.02, 0.04, 20)
+    assert np.all(np.abs(st["u"] - 0.625) <= 0.15)
+    e, _ = oracle_lib.tgv_solve(np.zeros(0, F.CUBE_DTYPE), np.zeros((0, 8), np.uint32), np.zeros(0, F.LEAF_DTYPE), "oc")
+    assert len(e) == 0
+
+
+def test_kat_stage5_stats_and_pyramid(oracle_lib):
+    """tests/test_stage5.cpp:21-41 and 84-101."""
+    b = np.zeros(8, np.uint32); b[4] = 10
+    assert abs(oracle_lib.median_indicator(b) - 0.125) < 0.01 and abs(oracle_lib.mean_indicator(b) - 0.125) < 0.01
+    b = np.zeros(8, np.uint32); b[3] = 5; b[4] = 5
+    assert abs(oracle_lib.median_indicator(b) + 0.125) < 0.01
+    z = np.zeros(8, np.uint32)
+    assert oracle_lib.median_indicator(z) == 0.0 and oracle_lib.mean_indicator(z) == 0.0
+    tex, dims = oracle_lib.pyramid(np.full((8, 8), 10.0, np.float32))
+    assert len(dims) >= 4 and [d[0] for d in dims[:3]] == [8, 4, 2]
+    assert np.all(tex == 10.0)
+
+
+def test_kat_stage5_project_and_plane(oracle_lib):
+    """tests/test_stage5.cpp:45-80 and 105-146 (identity camera at the origin)."""
+    m = dict(depth=np.full((32, 32), 5.0, np.float32), rt_inv=np.eye(4, dtype=np.float32), fx=100.0, fy=100.0,
+             cx=16.0, cy=16.0)
+    ok, lv, u, v, z = oracle_lib.project(m, (0.0, 0.0, 5.0), 0.04)
+    assert ok and abs(z - 5.0) <= 1e-4 and lv == 0
+    assert not oracle_lib.project(m, (0.0, 0.0, -1.0), 0.1)[0]
+    assert not oracle_lib.project(m, (1000.0, 0.0, 5.0), 0.1)[0]
+    ok, lv, *_ = oracle_lib.project(m, (0.0, 0.0, 1.0), 2.0)
+    assert ok and lv >= 1
+    plane = dict(depth=np.full((16, 16), 5.0, np.float32), rt_inv=np.eye(4, dtype=np.float32), fx=50.0, fy=50.0,
+                 cx=8.0, cy=8.0)
+    c = F.make_cubes([int(F.morton_encode(np.uint32(4 << 17), np.uint32(4 << 17), np.uint32(8 << 17)))], 4, 1 / 16)
+    h = oracle_lib.compute_histograms(c, [plane], (-0.5, -0.5, 4.0), 1.0)
+    assert h.sum() > 0 and h[0, :4].sum() > h[0, 4:].sum()

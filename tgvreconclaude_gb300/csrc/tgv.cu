@@ -1,0 +1,877 @@
+// Stage 6 on sm_103a: coarse-to-fine primal-dual TGV with a histogram data term
+// over a Morton-ordered octree (reference src/tgv.cpp).
+//
+// Device layout ("level-major"): cubes are stably bucketed by depth, so level
+// L's active cubes occupy one contiguous position range and keep their
+// (Morton) index order inside it.  Per position, structure-of-arrays:
+//   uv   float4 {u, vx, vy, vz}        bar  float4 {u_bar, vx_bar, vy_bar, vz_bar}
+//   P4   float4 {p0, p1, p2, q0}       Q4   float4 {q1, q2, q3, q4}     Q1 float {q5}
+//   dat  float2 {median, tau*tot or -1 for an empty histogram}
+//   nb   int32 [6][npos] neighbour positions (-1 none, BORDER flag), par int32
+// = 100 B of state per cube, every per-cube record a single vector access.
+//
+// Kernels (one thread per active cube, block-contiguous chunks):
+//   K3 setup: k_prep / k_bucket_* (stable counting sort) / k_hash_insert /
+//      k_neighbours<MODE> -- replaces CodeMap + NeighbourTable + the streaming
+//      path's on-disk lookups (tgv.cpp:97-133, 367-370, 651-688, 955-1021)
+//   K4 k_init -- median / data term once per solve instead of per iteration
+//      (prox_data, tgv.cpp:75-94)
+//   K5 k_parent_init / k_stream_snapshot -- level start (tgv.cpp:391-409,
+//      484-487, 878-937, 1029-1057)
+//   K6 k_dual<MODE>   -- p and q sweeps (tgv.cpp:158-189): 100 B/cube
+//   K7 k_primal<MODE> -- u, v and extrapolation sweeps (tgv.cpp:191-230): 104 B/cube
+//      Both optionally accumulate the FP64 residual sums of the stopping test.
+// The reference's five Jacobi sweeps are exact as two kernels: q reads only
+// the bars, which the p sweep does not write; u and v read only p/q, which
+// they do not write, and the extrapolation is per cube.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace tgvg {
+
+static constexpr int NBUCKET = 23;  // depths 0..21, 22 = never active
+static constexpr int SORT_BLOCK = 1024;
+static constexpr int ITER_BLOCK = 256;
+
+enum { M_INMEM = 0, M_OC = 1, M_STREAM = 2 };
+
+// ---------------------------------------------------------------- setup ---
+
+// keys, depth, flags: [0] unsorted, [1] bad depth, [2] min depth, [3] max depth
+__global__ void k_prep(int n, const uint4* __restrict__ cubes, unsigned long long* __restrict__ keys,
+                       int* __restrict__ depth, int* flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool v = i < n;
+    int lo = 21, hi = 0;
+    if (v) {
+        const uint4 c = cubes[i];
+        const unsigned long long k = ((unsigned long long)c.x << 32) | c.y;
+        keys[i] = k;
+        const int d = (int)c.w;
+        depth[i] = d;
+        if (d < 0 || d > 21) atomicOr(flags + 1, 1);
+        if (i > 0) {
+            const uint4 pc = cubes[i - 1];
+            const unsigned long long pk = ((unsigned long long)pc.x << 32) | pc.y;
+            if (pk > k) atomicOr(flags + 0, 1);
+        }
+        lo = hi = d;
+    }
+    // warp-reduced depth range (block size is a multiple of 32, all lanes present)
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0 && (blockIdx.x * blockDim.x + threadIdx.x) < n) {
+        atomicMin(flags + 2, lo);
+        atomicMax(flags + 3, hi);
+    }
+}
+
+// leaf_of[i] = caller index of the leaf holding cube i, or -1.  Leaves arrive
+// sorted by first index (non-overlapping) with their caller indices.
+__global__ void k_leaf_of(int n, int nleaf, const int* __restrict__ s_first,
+                          const int* __restrict__ s_last, const int* __restrict__ s_id,
+                          int* __restrict__ leaf_of) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int lo = 0, hi = nleaf;  // first s with s_first[s] > i
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s_first[mid] <= i) lo = mid + 1; else hi = mid;
+    }
+    const int s = lo - 1;
+    leaf_of[i] = (s >= 0 && i <= s_last[s]) ? s_id[s] : -1;
+}
+
+__device__ __forceinline__ int bucket_of(int mode, int d, int leaf) {
+    return (d < 0 || d > 21 || (mode == M_STREAM && leaf < 0)) ? 22 : d;
+}
+
+__global__ void k_bucket_count(int n, int mode, const int* __restrict__ depth,
+                               const int* __restrict__ leaf_of, int* __restrict__ counts, int nblk) {
+    __shared__ int sc[NBUCKET];
+    if (threadIdx.x < NBUCKET) sc[threadIdx.x] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * SORT_BLOCK + threadIdx.x;
+    if (i < n) atomicAdd(&sc[bucket_of(mode, depth[i], leaf_of[i])], 1);
+    __syncthreads();
+    if (threadIdx.x < NBUCKET) counts[threadIdx.x * nblk + blockIdx.x] = sc[threadIdx.x];
+}
+
+// In-place exclusive scan of counts[NBUCKET * nblk] (bucket-major), one block.
+// bstart[b] = first position of bucket b, bstart[NBUCKET] = n.
+__global__ void k_bucket_scan(int total, int* __restrict__ counts, int nblk, int* __restrict__ bstart) {
+    __shared__ int part[SORT_BLOCK];
+    const int t = threadIdx.x;
+    const int per = (total + SORT_BLOCK - 1) / SORT_BLOCK;
+    const int a = min(total, t * per), b = min(total, a + per);
+    int s = 0;
+    for (int k = a; k < b; ++k) s += counts[k];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < SORT_BLOCK; off <<= 1) {
+        int v = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = part[t] - s;  // exclusive
+    for (int k = a; k < b; ++k) { const int c = counts[k]; counts[k] = run; run += c; }
+    __syncthreads();
+    if (t < NBUCKET) bstart[t] = counts[t * nblk];
+    if (t == 0) bstart[NBUCKET] = part[SORT_BLOCK - 1];
+}
+
+// Stable scatter: rank inside the block = earlier warps' count + lanes below.
+__global__ void k_bucket_scatter(int n, int mode, const int* __restrict__ depth,
+                                 const int* __restrict__ leaf_of, const int* __restrict__ offs, int nblk,
+                                 int* __restrict__ perm, int* __restrict__ inv) {
+    __shared__ int wcnt[SORT_BLOCK / 32][NBUCKET];
+    const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+    const int i = blockIdx.x * SORT_BLOCK + t;
+    const int b = i < n ? bucket_of(mode, depth[i], leaf_of[i]) : NBUCKET;
+    for (int k = lane; k < NBUCKET; k += 32) wcnt[w][k] = 0;
+    __syncwarp();
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (b < NBUCKET && rank == 0) wcnt[w][b] = __popc(peers);
+    __syncthreads();
+    if (t < NBUCKET) {
+        int run = 0;
+        for (int ww = 0; ww < SORT_BLOCK / 32; ++ww) { const int c = wcnt[ww][t]; wcnt[ww][t] = run; run += c; }
+    }
+    __syncthreads();
+    if (i < n) {
+        const int pos = offs[b * nblk + blockIdx.x] + wcnt[w][b] + rank;
+        perm[pos] = i;
+        inv[i] = pos;
+    }
+}
+
+__global__ void k_hash_insert(int n, const unsigned long long* __restrict__ keys, HashView h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long key = keys[i];
+    uint64_t s = mix64(key) & h.mask;
+    for (uint64_t probe = 0; probe <= h.mask; ++probe) {
+        const unsigned long long prev = atomicCAS(h.keys + s, (unsigned long long)NO_KEY, key);
+        if (prev == (unsigned long long)NO_KEY || prev == key) {
+            atomicMin(h.rmin + s, i);
+            atomicMax(h.rmax + s, i);
+            return;
+        }
+        s = (s + 1) & h.mask;
+    }
+}
+
+// Resolve one neighbour code into a position (or -1), with the semantics of
+// the selected entry point.  INMEM/OC: largest index with the code, falling
+// back to the code of its parent (neighbor_idx_ctf, tgv.cpp:97-109); OC flags
+// neighbours of other leaves.  STREAM: the leaf's own largest index with the
+// code, else the cube file's bisection hit as a frozen border cube, else the
+// same two steps for the parent code (tgv.cpp:960-1021).
+template <int MODE>
+__device__ __forceinline__ int resolve(uint64_t nk, int d, int lid, int f0, int l0, const HashView& h,
+                                       int n, const int* __restrict__ inv, const int* __restrict__ leaf_of) {
+    if (nk == NO_KEY) return -1;
+    for (int step = 0; step < 2; ++step) {
+        if (step == 1) {
+            if (d <= 0) return -1;
+            nk = parent_key(nk, d);
+        }
+        const int s = hash_find(h, nk);
+        if (s < 0) continue;
+        const int r0 = h.rmin[s], r1 = h.rmax[s];
+        if (MODE == M_STREAM) {
+            const int hi = min(r1, l0);
+            if (max(r0, f0) <= hi) return inv[hi];
+            const int g = bisect_hit(n, r0, r1);
+            return g < 0 ? -1 : (inv[g] | BORDER);
+        } else {
+            int pos = inv[r1];
+            if (MODE == M_OC && leaf_of[r1] != lid) pos |= BORDER;
+            return pos;
+        }
+    }
+    return -1;
+}
+
+template <int MODE>
+__global__ void k_neighbours(int n_act, int n, const int* __restrict__ perm, const int* __restrict__ inv,
+                             const unsigned long long* __restrict__ keys, const int* __restrict__ depth,
+                             const int* __restrict__ leaf_of, const int* __restrict__ leaf_first,
+                             const int* __restrict__ leaf_last, HashView h, int npos,
+                             int* __restrict__ nb, int* __restrict__ par) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_act) return;
+    const int i = perm[p];
+    const uint64_t key = keys[i];
+    const int d = depth[i];
+    const int lid = leaf_of[i];
+    int f0 = 0, l0 = n - 1;
+    if (MODE == M_STREAM && lid >= 0) { f0 = leaf_first[lid]; l0 = leaf_last[lid]; }
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+        nb[f * npos + p] = resolve<MODE>(face_key(key, f, d), d, lid, f0, l0, h, n, inv, leaf_of);
+    int pp = -1;
+    if (d > 0) {
+        const int s = hash_find(h, parent_key(key, d));
+        if (s >= 0) {
+            const int j = (MODE == M_STREAM) ? bisect_hit(n, h.rmin[s], h.rmax[s]) : h.rmax[s];
+            pp = j >= 0 ? inv[j] : -1;
+        }
+    }
+    par[p] = pp;
+}
+
+// Data term and initial state (tgv.cpp:372-373, 384-385; prox_data 75-94).
+template <int NB>
+__global__ void k_init(int npos, const int* __restrict__ perm, const uint32_t* __restrict__ hists, int init,
+                       const float* __restrict__ u_init, const int* __restrict__ leaf_of,
+                       float4* __restrict__ uv, float4* __restrict__ bar, float4* __restrict__ P4,
+                       float4* __restrict__ Q4, float* __restrict__ Q1, float2* __restrict__ dat,
+                       int* __restrict__ lid) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npos) return;
+    const int i = perm[p];
+    const uint32_t* row = hists + (size_t)i * NB;
+    uint32_t b[NB];
+    uint32_t tot = 0;
+#pragma unroll
+    for (int k = 0; k < NB; ++k) { b[k] = row[k]; tot += b[k]; }
+    float med = 0.0f, shrink = -1.0f;
+    if (tot != 0) {
+        uint32_t cum = 0;
+        int km = NB;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            cum += b[k];
+            if (km == NB && cum * 2u >= tot) km = k;
+        }
+        med = km < NB ? fadd(-1.0f, fdiv(fadd((float)km, 0.5f), NB / 2.0f)) : 1.0f;
+        shrink = fmul(0.25f, (float)tot);
+    }
+    float u0 = init == TGVG_INIT_MEDIAN ? med : (init == TGVG_INIT_ZERO ? 0.0f : u_init[i]);
+    const float4 s = make_float4(u0, 0.f, 0.f, 0.f);
+    uv[p] = s;
+    bar[p] = s;
+    P4[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Q4[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Q1[p] = 0.f;
+    dat[p] = make_float2(med, shrink);
+    lid[p] = leaf_of[i];
+}
+
+// Per-(leaf, level) position ranges inside each level's segment, whose
+// positions are sorted by cube index: ranges[(leaf*NBUCKET + b)*2 + {0,1}].
+__global__ void k_leaf_ranges(int nleaf, const int* __restrict__ leaf_first, const int* __restrict__ leaf_last,
+                              const int* __restrict__ bstart, const int* __restrict__ perm,
+                              int* __restrict__ ranges) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nleaf * 22) return;
+    const int leaf = t / 22, b = t % 22;
+    const int s = bstart[b], e = bstart[b + 1];
+    const int f0 = leaf_first[leaf], l0 = leaf_last[leaf];
+    int lo = s, hi = e;
+    while (lo < hi) { const int m = (lo + hi) >> 1; if (perm[m] < f0) lo = m + 1; else hi = m; }
+    const int a = lo;
+    hi = e;
+    while (lo < hi) { const int m = (lo + hi) >> 1; if (perm[m] <= l0) lo = m + 1; else hi = m; }
+    ranges[(leaf * NBUCKET + b) * 2 + 0] = (l0 >= f0) ? a : s;
+    ranges[(leaf * NBUCKET + b) * 2 + 1] = (l0 >= f0) ? lo : s;
+}
+
+// ------------------------------------------------------------- per level ---
+
+__global__ void k_parent_init(int o, int n, const int* __restrict__ par, float4* __restrict__ uv,
+                              float4* __restrict__ bar, float4* __restrict__ P4, float4* __restrict__ Q4,
+                              float* __restrict__ Q1) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int p = o + t;
+    const int j = par[p];
+    float4 s = uv[p];
+    // A parent at this same level is a cube whose own parent lookup returns
+    // itself, so it never changes here and can be read concurrently.
+    if (j >= 0 && j != p) { s = uv[j]; uv[p] = s; }
+    bar[p] = s;
+    P4[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Q4[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Q1[p] = 0.f;
+}
+
+// Streaming level start: every cube's bars restart from its state u/v, and the
+// frozen copy for border reads is taken (build_bars_frozen, tgv.cpp:606-635).
+__global__ void k_stream_snapshot(int npos, const float4* __restrict__ uv, float4* __restrict__ bar,
+                                  float4* __restrict__ snap) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npos) return;
+    const float4 s = uv[p];
+    bar[p] = s;
+    snap[p] = s;
+}
+
+__global__ void k_copy4(int npos, const float4* __restrict__ src, float4* __restrict__ dst) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < npos) dst[p] = src[p];
+}
+
+struct IterArgs {
+    int o, n, chunk, npos;
+    const int* nb;
+    float4* uv;
+    float4* bar;
+    float4* P4;
+    float4* Q4;
+    float* Q1;
+    const float2* dat;
+    const float4* snap;
+    const int* lid;     // STREAM: stop/residual slot per position
+    double* acc;        // [slot][4]: d_primal, d_dual, n_primal, n_dual
+    const int* done;    // [slot]
+    int slot0;          // INMEM/OC: the slot of this launch
+    float alpha0, alpha1;
+};
+
+// Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
+// with one atomic per warp per slot run (positions are sorted by leaf).
+struct WarpAcc {
+    double x = 0.0, y = 0.0;
+    int cur = -1;
+    __device__ __forceinline__ void flush(double* acc, int k0, int lane) {
+        double a = x, b = y;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        if (lane == 0 && cur >= 0) {
+            atomicAdd(acc + cur * 4 + k0, a);
+            atomicAdd(acc + cur * 4 + k0 + 2, b);
+        }
+        x = 0.0; y = 0.0;
+    }
+    // slot: this lane's slot (-1 if the lane has no cube); whole warp calls.
+    __device__ __forceinline__ void add(int slot, double dx, double dy, double* acc, int k0, int lane) {
+        const int s0 = __shfl_sync(0xffffffffu, slot, __ffs(__ballot_sync(0xffffffffu, slot >= 0)) - 1);
+        const bool uniform = __all_sync(0xffffffffu, slot < 0 || slot == s0);
+        if (uniform) {
+            if (s0 != cur) { flush(acc, k0, lane); cur = s0; }
+            x += dx; y += dy;
+        } else if (slot >= 0) {
+            atomicAdd(acc + slot * 4 + k0, dx);
+            atomicAdd(acc + slot * 4 + k0 + 2, dy);
+        }
+    }
+};
+
+__device__ __forceinline__ void clip3(float& a, float& b, float& c, float r) {
+    const float n2 = fadd(fadd(fmul(a, a), fmul(b, b)), fmul(c, c));
+    if (n2 > fmul(r, r)) {
+        const float s = fdiv(r, fsqrt(n2));
+        a = fmul(a, s); b = fmul(b, s); c = fmul(c, s);
+    }
+}
+__device__ __forceinline__ void clip6(float* q, float r) {
+    float n2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) n2 = fadd(n2, fmul(q[k], q[k]));
+    if (n2 > fmul(r, r)) {
+        const float s = fdiv(r, fsqrt(n2));
+#pragma unroll
+        for (int k = 0; k < 6; ++k) q[k] = fmul(q[k], s);
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const float4* __restrict__ bar,
+                                            const float4* __restrict__ snap) {
+    if (j < 0) return own;
+    if (MODE != M_INMEM && (j & BORDER)) return snap[j & POS_MASK];
+    return bar[j];
+}
+
+// K6: dual ascent on p (|grad u - v|, radius alpha1) and q (|e(v)|, radius alpha0).
+template <int MODE, bool RES, bool STOP>
+__global__ void __launch_bounds__(ITER_BLOCK) k_dual(IterArgs a) {
+    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int beg = a.o + blockIdx.x * a.chunk;
+    const int end = min(a.o + a.n, beg + a.chunk);
+    WarpAcc wa;
+    for (int g = beg + warp * 32; g < end; g += ITER_BLOCK) {
+        const int p = g + lane;
+        int slot = -1;
+        if (p < end) slot = (MODE == M_STREAM) ? a.lid[p] : a.slot0;
+        bool work = p < end;
+        if (STOP && work && MODE == M_STREAM) work = !a.done[slot];
+        double dd = 0.0, nd = 0.0;
+        if (work) {
+            const float4 b = a.bar[p];
+            const int j0 = a.nb[p], j2 = a.nb[2 * a.npos + p], j4 = a.nb[4 * a.npos + p];
+            const float4 B0 = fetch_bar<MODE>(j0, b, a.bar, a.snap);
+            const float4 B2 = fetch_bar<MODE>(j2, b, a.bar, a.snap);
+            const float4 B4 = fetch_bar<MODE>(j4, b, a.bar, a.snap);
+            const float4 P = a.P4[p];
+            const float4 Q = a.Q4[p];
+            const float q5o = a.Q1[p];
+            float p0 = fadd(P.x, fmul(0.25f, fsub(fsub(B0.x, b.x), b.y)));
+            float p1 = fadd(P.y, fmul(0.25f, fsub(fsub(B2.x, b.x), b.z)));
+            float p2 = fadd(P.z, fmul(0.25f, fsub(fsub(B4.x, b.x), b.w)));
+            clip3(p0, p1, p2, a.alpha1);
+            const float e0 = fsub(B0.y, b.y);
+            const float e1 = fsub(B2.z, b.z);
+            const float e2 = fsub(B4.w, b.w);
+            const float e3 = fmul(0.5f, fsub(fadd(fsub(B2.y, b.y), B0.z), b.z));
+            const float e4 = fmul(0.5f, fsub(fadd(fsub(B4.y, b.y), B0.w), b.w));
+            const float e5 = fmul(0.5f, fsub(fadd(fsub(B4.z, b.z), B2.w), b.w));
+            float q[6] = {fadd(P.w, fmul(0.25f, e0)), fadd(Q.x, fmul(0.25f, e1)), fadd(Q.y, fmul(0.25f, e2)),
+                          fadd(Q.z, fmul(0.25f, e3)), fadd(Q.w, fmul(0.25f, e4)), fadd(q5o, fmul(0.25f, e5))};
+            clip6(q, a.alpha0);
+            a.P4[p] = make_float4(p0, p1, p2, q[0]);
+            a.Q4[p] = make_float4(q[1], q[2], q[3], q[4]);
+            a.Q1[p] = q[5];
+            if (RES) {
+                const double d0 = (double)p0 - P.x, d1 = (double)p1 - P.y, d2 = (double)p2 - P.z;
+                const double d3 = (double)q[0] - P.w, d4 = (double)q[1] - Q.x, d5 = (double)q[2] - Q.y;
+                const double d6 = (double)q[3] - Q.z, d7 = (double)q[4] - Q.w, d8 = (double)q[5] - q5o;
+                dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5 + d6 * d6 + d7 * d7 + d8 * d8;
+                nd = (double)p0 * p0 + (double)p1 * p1 + (double)p2 * p2;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) nd += (double)q[k] * q[k];
+            }
+        }
+        if (RES) wa.add(work ? slot : -1, dd, nd, a.acc, 1, lane);
+    }
+    if (RES) wa.flush(a.acc, 1, lane);
+}
+
+// K7: primal descent on u (prox of tot*|u - median|) and v, then extrapolation.
+template <int MODE, bool RES, bool STOP>
+__global__ void __launch_bounds__(ITER_BLOCK) k_primal(IterArgs a) {
+    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int beg = a.o + blockIdx.x * a.chunk;
+    const int end = min(a.o + a.n, beg + a.chunk);
+    WarpAcc wa;
+    for (int g = beg + warp * 32; g < end; g += ITER_BLOCK) {
+        const int p = g + lane;
+        int slot = -1;
+        if (p < end) slot = (MODE == M_STREAM) ? a.lid[p] : a.slot0;
+        bool work = p < end;
+        if (STOP && work && MODE == M_STREAM) work = !a.done[slot];
+        double dd = 0.0, nd = 0.0;
+        if (work) {
+            const float4 U = a.uv[p];
+            const float4 P = a.P4[p];
+            const float4 Q = a.Q4[p];
+            const float q5 = a.Q1[p];
+            const float2 D = a.dat[p];
+            const int j1 = a.nb[a.npos + p], j3 = a.nb[3 * a.npos + p], j5 = a.nb[5 * a.npos + p];
+            float gp10 = 0.f, gq10 = 0.f, gq13 = 0.f, gq14 = 0.f;
+            float gp31 = 0.f, gq31 = 0.f, gq33 = 0.f, gq35 = 0.f;
+            float gp52 = 0.f, gq52 = 0.f, gq54 = 0.f, gq55 = 0.f;
+            if (j1 >= 0 && !(MODE == M_STREAM && (j1 & BORDER))) {
+                const int j = j1 & POS_MASK;
+                const float4 a4 = a.P4[j], b4 = a.Q4[j];
+                gp10 = a4.x; gq10 = a4.w; gq13 = b4.z; gq14 = b4.w;
+            }
+            if (j3 >= 0 && !(MODE == M_STREAM && (j3 & BORDER))) {
+                const int j = j3 & POS_MASK;
+                const float4 a4 = a.P4[j], b4 = a.Q4[j];
+                gp31 = a4.y; gq31 = b4.x; gq33 = b4.z; gq35 = a.Q1[j];
+            }
+            if (j5 >= 0 && !(MODE == M_STREAM && (j5 & BORDER))) {
+                const int j = j5 & POS_MASK;
+                const float4 a4 = a.P4[j], b4 = a.Q4[j];
+                gp52 = a4.z; gq52 = b4.y; gq54 = b4.w; gq55 = a.Q1[j];
+            }
+            const float p0 = P.x, p1 = P.y, p2 = P.z;
+            const float q0 = P.w, q1 = Q.x, q2 = Q.y, q3 = Q.z, q4 = Q.w;
+            const float div_p = fadd(fadd(fsub(p0, gp10), fsub(p1, gp31)), fsub(p2, gp52));
+            const float z = fadd(U.x, fmul(0.25f, div_p));
+            float un;
+            if (D.y < 0.0f) {
+                un = z;
+            } else {
+                const float diff = fsub(z, D.x);
+                if (diff > D.y) un = fsub(z, D.y);
+                else if (diff < -D.y) un = fadd(z, D.y);
+                else un = D.x;
+            }
+            const float dqx = fadd(fadd(fsub(q0, gq10), fsub(q3, gq33)), fsub(q4, gq54));
+            const float dqy = fadd(fadd(fsub(q3, gq13), fsub(q1, gq31)), fsub(q5, gq55));
+            const float dqz = fadd(fadd(fsub(q4, gq14), fsub(q5, gq35)), fsub(q2, gq52));
+            const float vxn = fadd(U.y, fmul(0.25f, fadd(p0, dqx)));
+            const float vyn = fadd(U.z, fmul(0.25f, fadd(p1, dqy)));
+            const float vzn = fadd(U.w, fmul(0.25f, fadd(p2, dqz)));
+            a.bar[p] = make_float4(fsub(fmul(2.0f, un), U.x), fsub(fmul(2.0f, vxn), U.y),
+                                   fsub(fmul(2.0f, vyn), U.z), fsub(fmul(2.0f, vzn), U.w));
+            a.uv[p] = make_float4(un, vxn, vyn, vzn);
+            if (RES) {
+                const double d0 = (double)un - U.x, d1 = (double)vxn - U.y, d2 = (double)vyn - U.z,
+                             d3 = (double)vzn - U.w;
+                dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
+                nd = (double)un * un + (double)vxn * vxn + (double)vyn * vyn + (double)vzn * vzn;
+            }
+        }
+        if (RES) wa.add(work ? slot : -1, dd, nd, a.acc, 0, lane);
+    }
+    if (RES) wa.flush(a.acc, 0, lane);
+}
+
+// Stopping test after a residual iteration: relative fixed-point residual
+// (|x+ - x| + |y+ - y|) / (|x+| + |y+|) in FP64 per slot (sigma = tau).
+__global__ void k_check(int nslot, double* __restrict__ acc, int* __restrict__ done, float tol, int iter,
+                        int* __restrict__ iters_run, double* __restrict__ resid) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslot || done[s]) return;
+    double* q = acc + s * 4;
+    const double num = sqrt(q[0]) + sqrt(q[1]);
+    const double den = sqrt(q[2]) + sqrt(q[3]);
+    const double rel = den > 0.0 ? num / den : 0.0;
+    resid[s] = rel;
+    if (rel <= (double)tol) { done[s] = 1; iters_run[s] = iter + 1; }
+    q[0] = q[1] = q[2] = q[3] = 0.0;
+}
+
+__global__ void k_unpermute(int n, const int* __restrict__ inv, const float4* __restrict__ uv,
+                            const float4* __restrict__ P4, const float4* __restrict__ Q4,
+                            const float* __restrict__ Q1, float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int p = inv[i];
+    const float4 u = uv[p], a = P4[p], b = Q4[p];
+    float* r = out + (size_t)i * 13;
+    r[0] = u.x; r[1] = u.y; r[2] = u.z; r[3] = u.w;
+    r[4] = a.x; r[5] = a.y; r[6] = a.z; r[7] = a.w;
+    r[8] = b.x; r[9] = b.y; r[10] = b.z; r[11] = b.w;
+    r[12] = Q1[p];
+}
+
+// ------------------------------------------------------------------ host ---
+
+static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+template <int MODE>
+static void launch_iter(tgvg_ctx* ctx, const IterArgs& a, bool res, bool stop, bool dual) {
+    const unsigned grid = (unsigned)((a.n + a.chunk - 1) / a.chunk);
+#define TGVG_ITER(K)                                                                  \
+    if (res && stop) K<MODE, true, true><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);    \
+    else if (res) K<MODE, true, false><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);      \
+    else if (stop) K<MODE, false, true><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);     \
+    else K<MODE, false, false><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);
+    if (dual) { TGVG_ITER(k_dual) } else { TGVG_ITER(k_primal) }
+#undef TGVG_ITER
+}
+
+int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists, int64_t n64,
+                  int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, int32_t mode,
+                  const tgvg_params* prm, const float* d_u_init, tgvg_state* d_out, tgvg_stats* stats) {
+    tgvg_stats st;
+    std::memset(&st, 0, sizeof(st));
+    const int64_t k0 = ctx->kernels;
+    if (mode < 0 || mode > 2 || (nbins != 8 && nbins != 10) || !prm || n64 < 0 || n64 > POS_MASK)
+        return TGVG_ERR_INVALID;
+    if (prm->init < 0 || prm->init > 2 || (prm->init == TGVG_INIT_GIVEN && n64 > 0 && !d_u_init))
+        return TGVG_ERR_INVALID;
+    if (mode != M_INMEM && nleaf > 0 && !leaves) return TGVG_ERR_INVALID;
+    const int n = (int)n64;
+    if (n == 0) { if (stats) *stats = st; return TGVG_OK; }
+    if (!d_cubes || !d_hists || !d_out) return TGVG_ERR_INVALID;
+
+    // ---- leaves: clamp like load_cubes_range (octree_builder.cpp:131-135), sort, reject overlap
+    std::vector<int> lf, ll;  // by caller index (empty leaf: first > last)
+    if (mode == M_INMEM) {
+        lf.assign(1, 0); ll.assign(1, n - 1);
+    } else {
+        lf.resize(std::max(0, nleaf)); ll.resize(std::max(0, nleaf));
+        for (int l = 0; l < nleaf; ++l) {
+            const uint32_t a = leaves[l].first_idx, b = leaves[l].last_idx;
+            if (int64_t(a) >= n || a > b) { lf[l] = 1; ll[l] = 0; continue; }
+            lf[l] = (int)a;
+            ll[l] = (int)std::min<int64_t>(int64_t(b), n - 1);
+        }
+    }
+    const int L = (int)lf.size();
+    std::vector<int> order;
+    for (int l = 0; l < L; ++l) if (lf[l] <= ll[l]) order.push_back(l);
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return lf[x] < lf[y]; });
+    for (size_t k = 1; k < order.size(); ++k)
+        if (lf[order[k]] <= ll[order[k - 1]]) return TGVG_ERR_OVERLAP;
+    std::vector<int> s_first, s_last, s_id;
+    for (int l : order) { s_first.push_back(lf[l]); s_last.push_back(ll[l]); s_id.push_back(l); }
+    const int nsl = (int)s_first.size();
+    const int nslot = std::max(1, L);
+
+    cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1], e2 = ctx->ev[2];
+    TGVG_CK(ctx, cudaEventRecord(e0, ctx->stream));
+
+    // ---- buffers
+    const int nblk = (n + SORT_BLOCK - 1) / SORT_BLOCK;
+    uint64_t cap = 1024;
+    while (cap < 2ull * (uint64_t)n) cap <<= 1;
+    auto B = [&](int id, size_t bytes) { return ctx->buf(id, bytes); };
+    auto* keys = (unsigned long long*)B(B_KEYS, 8ull * n);
+    auto* depth = (int*)B(B_DEPTH, 4ull * n);
+    auto* leaf_of = (int*)B(B_LEAFOF, 4ull * n);
+    auto* counts = (int*)B(B_BCOUNT, 4ull * NBUCKET * nblk);
+    auto* bstart = (int*)B(B_BTOT, 4ull * (NBUCKET + 1));
+    auto* perm = (int*)B(B_PERM, 4ull * n);
+    auto* inv = (int*)B(B_INV, 4ull * n);
+    auto* hk = (unsigned long long*)B(B_HKEYS, 8ull * cap);
+    auto* hmin = (int*)B(B_HMIN, 4ull * cap);
+    auto* hmax = (int*)B(B_HMAX, 4ull * cap);
+    auto* nb = (int*)B(B_NB, 4ull * 6 * n);
+    auto* par = (int*)B(B_PAR, 4ull * n);
+    auto* uv = (float4*)B(B_UV, 16ull * n);
+    auto* bar = (float4*)B(B_BAR, 16ull * n);
+    auto* P4 = (float4*)B(B_P4, 16ull * n);
+    auto* Q4 = (float4*)B(B_Q4, 16ull * n);
+    auto* Q1 = (float*)B(B_Q1, 4ull * n);
+    auto* dat = (float2*)B(B_DAT, 8ull * n);
+    auto* snap = (float4*)B(B_SNAP, mode == M_INMEM ? 16 : 16ull * n);
+    auto* lid = (int*)B(B_LID, 4ull * n);
+    auto* lv = (int*)B(B_LEAVES, 4ull * (3 * std::max(1, nsl) + 2 * std::max(1, L)));
+    auto* acc = (double*)B(B_ACC, 32ull * nslot);
+    auto* flags = (int*)B(B_FLAGS, 4ull * (8 + 2 * nslot));
+    auto* ranges = (int*)B(B_RANGES, 8ull * NBUCKET * std::max(1, L));
+    auto* resid = (double*)B(B_RESID, 8ull * nslot);
+    if (!keys || !depth || !leaf_of || !counts || !bstart || !perm || !inv || !hk || !hmin || !hmax ||
+        !nb || !par || !uv || !bar || !P4 || !Q4 || !Q1 || !dat || !snap || !lid || !lv || !acc ||
+        !flags || !ranges || !resid)
+        return TGVG_ERR_NOMEM;
+    int* d_sfirst = lv;
+    int* d_slast = lv + std::max(1, nsl);
+    int* d_sid = lv + 2 * std::max(1, nsl);
+    int* d_lfirst = lv + 3 * std::max(1, nsl);
+    int* d_llast = d_lfirst + std::max(1, L);
+    int* done = flags + 8;
+    int* iters_run = flags + 8 + nslot;
+
+    std::vector<int> hostleaf(3 * std::max(1, nsl) + 2 * std::max(1, L), 0);
+    for (int k = 0; k < nsl; ++k) {
+        hostleaf[k] = s_first[k];
+        hostleaf[std::max(1, nsl) + k] = s_last[k];
+        hostleaf[2 * std::max(1, nsl) + k] = s_id[k];
+    }
+    for (int l = 0; l < L; ++l) {
+        hostleaf[3 * std::max(1, nsl) + l] = lf[l];
+        hostleaf[3 * std::max(1, nsl) + std::max(1, L) + l] = ll[l];
+    }
+    TGVG_CK(ctx, cudaMemcpyAsync(lv, hostleaf.data(), 4 * hostleaf.size(), cudaMemcpyHostToDevice, ctx->stream));
+    const int init_flags[4] = {0, 0, 21, 0};
+    TGVG_CK(ctx, cudaMemcpyAsync(flags, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice, ctx->stream));
+
+    // ---- K3: keys, leaves, level-major order, hash, neighbours
+    k_prep<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, reinterpret_cast<const uint4*>(d_cubes), keys,
+                                                         depth, flags);
+    TGVG_LAUNCHED(ctx);
+    k_leaf_of<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, nsl, d_sfirst, d_slast, d_sid, leaf_of);
+    TGVG_LAUNCHED(ctx);
+    k_bucket_count<<<nblk, SORT_BLOCK, 0, ctx->stream>>>(n, mode, depth, leaf_of, counts, nblk);
+    TGVG_LAUNCHED(ctx);
+    k_bucket_scan<<<1, SORT_BLOCK, 0, ctx->stream>>>(NBUCKET * nblk, counts, nblk, bstart);
+    TGVG_LAUNCHED(ctx);
+    k_bucket_scatter<<<nblk, SORT_BLOCK, 0, ctx->stream>>>(n, mode, depth, leaf_of, counts, nblk, perm, inv);
+    TGVG_LAUNCHED(ctx);
+    int h_flags[4], h_bstart[NBUCKET + 1];
+    TGVG_CK(ctx, cudaMemcpyAsync(h_flags, flags, sizeof(h_flags), cudaMemcpyDeviceToHost, ctx->stream));
+    TGVG_CK(ctx, cudaMemcpyAsync(h_bstart, bstart, sizeof(h_bstart), cudaMemcpyDeviceToHost, ctx->stream));
+    TGVG_CK(ctx, cudaMemsetAsync(hk, 0xff, 8ull * cap, ctx->stream));
+    TGVG_CK(ctx, cudaMemsetAsync(hmin, 0x7f, 4ull * cap, ctx->stream));
+    TGVG_CK(ctx, cudaMemsetAsync(hmax, 0xff, 4ull * cap, ctx->stream));
+    HashView hv{hk, hmin, hmax, cap - 1};
+    k_hash_insert<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, keys, hv);
+    TGVG_LAUNCHED(ctx);
+    TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h_flags[1]) return ctx->fail(TGVG_ERR_INVALID, "cube depth outside 0..21");
+    if (mode == M_STREAM && h_flags[0])
+        return ctx->fail(TGVG_ERR_UNSORTED, "streaming semantics need Morton-sorted cubes");
+    const int min_d = h_flags[2], max_d = h_flags[3];
+    const int n_act = h_bstart[22];
+
+    if (n_act > 0) {
+        if (mode == M_INMEM)
+            k_neighbours<M_INMEM><<<blocks_for(n_act, 256), 256, 0, ctx->stream>>>(
+                n_act, n, perm, inv, keys, depth, leaf_of, d_lfirst, d_llast, hv, n, nb, par);
+        else if (mode == M_OC)
+            k_neighbours<M_OC><<<blocks_for(n_act, 256), 256, 0, ctx->stream>>>(
+                n_act, n, perm, inv, keys, depth, leaf_of, d_lfirst, d_llast, hv, n, nb, par);
+        else
+            k_neighbours<M_STREAM><<<blocks_for(n_act, 256), 256, 0, ctx->stream>>>(
+                n_act, n, perm, inv, keys, depth, leaf_of, d_lfirst, d_llast, hv, n, nb, par);
+        TGVG_LAUNCHED(ctx);
+    }
+    if (nbins == 8)
+        k_init<8><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, perm, d_hists, prm->init, d_u_init, leaf_of,
+                                                               uv, bar, P4, Q4, Q1, dat, lid);
+    else
+        k_init<10><<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, perm, d_hists, prm->init, d_u_init, leaf_of,
+                                                                uv, bar, P4, Q4, Q1, dat, lid);
+    TGVG_LAUNCHED(ctx);
+    std::vector<int> h_ranges;
+    if (mode != M_INMEM && L > 0) {
+        k_leaf_ranges<<<blocks_for(int64_t(L) * 22, 128), 128, 0, ctx->stream>>>(L, d_lfirst, d_llast, bstart,
+                                                                                perm, ranges);
+        TGVG_LAUNCHED(ctx);
+        h_ranges.resize(2ull * NBUCKET * L);
+        TGVG_CK(ctx, cudaMemcpyAsync(h_ranges.data(), ranges, 4 * h_ranges.size(), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    TGVG_CK(ctx, cudaEventRecord(e1, ctx->stream));
+
+    // ---- levels
+    const bool stop = prm->tol > 0.0f && prm->check_every > 0;
+    const int iters = std::max(0, prm->iters);
+    const int per_sm = 8;
+    st.min_depth = min_d;
+    st.max_depth = max_d;
+    std::vector<int> h_iters(nslot);
+    std::vector<double> h_res(nslot);
+    // optional per-launch timing of the largest level (not for sequential OC leaves)
+    int t_level = -1;
+    if (ctx->timing && mode != M_OC && iters > 0) {
+        int best = 0;
+        for (int Ld = min_d; Ld <= max_d; ++Ld)
+            if (h_bstart[Ld + 1] - h_bstart[Ld] > best) { best = h_bstart[Ld + 1] - h_bstart[Ld]; t_level = Ld; }
+        while ((int)ctx->tev.size() < 3 * iters) {
+            cudaEvent_t e;
+            TGVG_CK(ctx, cudaEventCreate(&e));
+            ctx->tev.push_back(e);
+        }
+    }
+    for (int Ld = min_d; Ld <= max_d; ++Ld) {
+        const int o = h_bstart[Ld], cnt = h_bstart[Ld + 1] - h_bstart[Ld];
+        if (cnt <= 0) continue;
+        if (Ld > min_d) {
+            k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, par, uv, bar, P4, Q4, Q1);
+            TGVG_LAUNCHED(ctx);
+        }
+        if (mode == M_STREAM) {
+            k_stream_snapshot<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, uv, bar, snap);
+            TGVG_LAUNCHED(ctx);
+        } else if (mode == M_OC) {
+            k_copy4<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, bar, snap);
+            TGVG_LAUNCHED(ctx);
+        }
+        // launch units: INMEM / STREAM the whole level; OC one per leaf, in caller order
+        struct Unit { int slot, o, n; };
+        std::vector<Unit> us;
+        if (mode == M_OC) {
+            for (int l = 0; l < L; ++l) {
+                const int a0 = h_ranges[(l * NBUCKET + Ld) * 2], a1 = h_ranges[(l * NBUCKET + Ld) * 2 + 1];
+                if (a1 > a0) us.push_back({l, a0, a1 - a0});
+            }
+        } else {
+            us.push_back({0, o, cnt});
+        }
+        if (stop) {
+            TGVG_CK(ctx, cudaMemsetAsync(acc, 0, 32ull * nslot, ctx->stream));
+            TGVG_CK(ctx, cudaMemsetAsync(done, 0, 4ull * nslot, ctx->stream));
+            std::vector<int> full(nslot, iters);
+            TGVG_CK(ctx, cudaMemcpyAsync(iters_run, full.data(), 4ull * nslot, cudaMemcpyHostToDevice,
+                                         ctx->stream));
+            TGVG_CK(ctx, cudaMemsetAsync(resid, 0, 8ull * nslot, ctx->stream));
+        }
+        for (const Unit& u : us) {
+            IterArgs a;
+            a.o = u.o; a.n = u.n; a.npos = n;
+            const int want = std::max(1, std::min((u.n + ITER_BLOCK - 1) / ITER_BLOCK, ctx->sm_count * per_sm));
+            a.chunk = ((u.n + want - 1) / want + 31) / 32 * 32;
+            a.nb = nb; a.uv = uv; a.bar = bar; a.P4 = P4; a.Q4 = Q4; a.Q1 = Q1; a.dat = dat; a.snap = snap;
+            a.lid = lid; a.acc = acc; a.done = done; a.slot0 = u.slot;
+            a.alpha0 = prm->alpha0; a.alpha1 = prm->alpha1;
+            const bool timed = Ld == t_level;
+            for (int it = 0; it < iters; ++it) {
+                const bool res = stop && ((it + 1) % prm->check_every == 0 || it + 1 == iters);
+                if (timed) cudaEventRecord(ctx->tev[3 * it], ctx->stream);
+                if (mode == M_INMEM) launch_iter<M_INMEM>(ctx, a, res, stop, true);
+                else if (mode == M_OC) launch_iter<M_OC>(ctx, a, res, stop, true);
+                else launch_iter<M_STREAM>(ctx, a, res, stop, true);
+                if (timed) cudaEventRecord(ctx->tev[3 * it + 1], ctx->stream);
+                if (mode == M_INMEM) launch_iter<M_INMEM>(ctx, a, res, stop, false);
+                else if (mode == M_OC) launch_iter<M_OC>(ctx, a, res, stop, false);
+                else launch_iter<M_STREAM>(ctx, a, res, stop, false);
+                if (timed) cudaEventRecord(ctx->tev[3 * it + 2], ctx->stream);
+                cudaError_t le = cudaGetLastError();
+                if (le != cudaSuccess) return ctx->cuda_fail(le, "iteration launch");
+                ctx->kernels += 2;
+                if (res) {
+                    k_check<<<blocks_for(nslot, 128), 128, 0, ctx->stream>>>(nslot, acc, done, prm->tol, it,
+                                                                             iters_run, resid);
+                    TGVG_LAUNCHED(ctx);
+                }
+            }
+        }
+        // level stats
+        if (st.n_levels < TGVG_MAX_LEVELS) {
+            const int k = st.n_levels++;
+            st.depth[k] = Ld;
+            st.active[k] = cnt;
+            if (stop) {
+                TGVG_CK(ctx, cudaMemcpyAsync(h_iters.data(), iters_run, 4ull * nslot, cudaMemcpyDeviceToHost,
+                                             ctx->stream));
+                TGVG_CK(ctx, cudaMemcpyAsync(h_res.data(), resid, 8ull * nslot, cudaMemcpyDeviceToHost,
+                                             ctx->stream));
+                TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+                int itmax = 0;
+                double rmax = 0.0;
+                int64_t li = 0;
+                if (mode == M_INMEM) {
+                    itmax = h_iters[0]; rmax = h_res[0]; li = int64_t(cnt) * itmax;
+                } else {
+                    for (int l = 0; l < L; ++l) {
+                        const int a0 = h_ranges[(l * NBUCKET + Ld) * 2], a1 = h_ranges[(l * NBUCKET + Ld) * 2 + 1];
+                        if (a1 <= a0) continue;
+                        itmax = std::max(itmax, h_iters[l]);
+                        rmax = std::max(rmax, h_res[l]);
+                        li += int64_t(a1 - a0) * h_iters[l];
+                    }
+                }
+                st.iters_run[k] = itmax;
+                st.residual[k] = rmax;
+                st.leaf_iters += li;
+            } else {
+                st.iters_run[k] = iters;
+                st.leaf_iters += int64_t(cnt) * iters;
+            }
+        }
+    }
+    TGVG_CK(ctx, cudaEventRecord(e2, ctx->stream));
+    k_unpermute<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, inv, uv, P4, Q4, Q1, reinterpret_cast<float*>(d_out));
+    TGVG_LAUNCHED(ctx);
+    TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    float ms_setup = 0.f, ms_iter = 0.f;
+    cudaEventElapsedTime(&ms_setup, e0, e1);
+    cudaEventElapsedTime(&ms_iter, e1, e2);
+    st.setup_ms = ms_setup;
+    st.iterate_ms = ms_iter;
+    st.total_ms = ms_setup + ms_iter;
+    st.kernel_launches = (int32_t)(ctx->kernels - k0);
+    if (t_level >= 0) {
+        double dsum = 0.0, psum = 0.0;
+        for (int it = 0; it < iters; ++it) {
+            float a = 0.f, b = 0.f;
+            cudaEventElapsedTime(&a, ctx->tev[3 * it], ctx->tev[3 * it + 1]);
+            cudaEventElapsedTime(&b, ctx->tev[3 * it + 1], ctx->tev[3 * it + 2]);
+            dsum += a;
+            psum += b;
+        }
+        st.kt_depth = t_level;
+        st.kt_launches = iters;
+        st.kt_active = h_bstart[t_level + 1] - h_bstart[t_level];
+        st.kt_dual_ms = dsum;
+        st.kt_primal_ms = psum;
+    }
+    if (stats) *stats = st;
+    return TGVG_OK;
+}
+
+}  // namespace tgvg
