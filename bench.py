@@ -1,0 +1,396 @@
+#!/usr/bin/env python3
+"""Benchmark: TGV leaf-iterations per second of the sm_103a Stage-6 solver.
+
+One step = one full coarse-to-fine solve (setup + every level, fixed iteration
+count per level) over one synthetic workload with inputs resident in HBM.  The
+default workload, three64, has the shape of the "plain method at scale"
+configuration: a sphere, a box and a torus seen by 64 cameras at 1920x1080,
+cubes to depth 11 (about 20M), 10-bin histograms from this package's own
+kernels, alpha1 = 1, alpha0 = 2, 1000 iterations per level.
+
+Also reported in the same JSON line:
+  e2e           the same metric through the public host-buffer C ABI call
+                (tgvg_tgv_minimize) from pinned host memory, copies included
+  roofline      the dominant iteration kernel timed per launch with CUDA events
+                on the library's stream, against MEASURED_PEAKS.json
+  cpu_baseline  the CPU oracle port on a bounded sample of the same workload
+  histograms    the Stage-5 pass (pyramids + binning) on the same workload
+
+`--impl reference` times the CPU implementation of the path (the oracle port of
+the reference's tgv.cpp, all host threads) on a bounded sample of the same
+workload and prints the same metric.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import glob
+import json
+import math
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "TGV leaf-iter/s"
+UNIT = "leaf-iter/s"
+BYTES_DUAL = 100     # per cube: bars 16 + neighbour ids 12 + p/q 36 read, p/q 36 written
+BYTES_PRIMAL = 104   # per cube: u/v 16 + p/q 36 + data 8 + neighbour ids 12 read, u/v 16 + bars 16 written
+BYTES_ITER = 168     # algorithmic bytes per leaf-iteration (one fused pass)
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_cube():
+    """dram bytes per cube per launch from the committed ncu summaries
+    (lines 'traffic_per_cube <kernel> <bytes>')."""
+    out = {}
+    for p in glob.glob(os.path.join(HERE, "profiles", "*.md")) + glob.glob(os.path.join(HERE, "profiles", "*.txt")):
+        with open(p) as f:
+            for line in f:
+                m = re.match(r"\s*traffic_per_cube\s+(\w+)\s+([0-9.eE+]+)", line)
+                if m:
+                    out[m.group(1)] = float(m.group(2))
+    return out
+
+
+class Clocks:
+    """nvidia-smi sampling (200 ms) during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("TGV_BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def allreduce_max(x, pg, torch):
+    if pg is None:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(x, pg, torch):
+    if pg is None:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t)
+    return float(t.item())
+
+
+def cpu_sample(w, n_sample: int, iters: int):
+    """A contiguous Morton-ordered slice of the workload (a spatially compact
+    region, like one treetop chunk)."""
+    n = min(n_sample, len(w.cubes))
+    start = max(0, (len(w.cubes) - n) // 2)
+    return w.cubes[start:start + n].copy(), w.hists[start:start + n].copy()
+
+
+def time_cpu_oracle(cubes, hists, iters, nthreads, repeats=1):
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+    oracle.build()
+    best = None
+    li = 0
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        _, st = oracle.tgv_solve(cubes, hists, None, "inmem", 2.0, 1.0, iters, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        li = sum(s["active"] * s["iters_run"] for s in st)
+        best = dt if best is None else min(best, dt)
+    return li / best, best, li
+
+
+def run_reference(args):
+    """CPU implementation of the path on the host cores (oracle port of the
+    reference's tgv_minimize; the reference itself is not compiled on this machine)."""
+    import torch
+    ws, rank, local, pg = dist_setup()
+    if rank != 0:
+        return 0
+    from tgvreconclaude_gb300 import workloads
+    torch.cuda.set_device(local)
+    # Scene and cubes come from torch on the GPU (input preparation only); the
+    # sample's histograms come from the CPU oracle, so no kernel of this
+    # package runs on this arm.
+    w = workloads.build(args.workload, seed=args.seed, device="cuda", histograms=False)
+    threads = os.cpu_count() or 1
+    cubes, _ = cpu_sample(w, args.ref_sample, args.cpu_iters)
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+    oracle.build()
+    maps = []
+    for c, d in zip(w.cams, w.depths):
+        maps.append(dict(depth=d, rt_inv=np.array(c.rt_inv[:], np.float32).reshape(4, 4), fx=c.fx, fy=c.fy, cx=c.cx,
+                         cy=c.cy, lidar=bool(c.lidar)))
+    hists = oracle.compute_histograms(cubes, maps, w.cfg["origin"], w.cfg["r_root"], nbins=w.cfg["nbins"],
+                                      nthreads=threads)
+    for _ in range(max(0, args.warmup)):
+        time_cpu_oracle(cubes, hists, args.cpu_iters, threads)
+    vals, tot_li, tot_t = [], 0, 0.0
+    for _ in range(args.steps):
+        v, dt, li = time_cpu_oracle(cubes, hists, args.cpu_iters, threads)
+        vals.append(v)
+        tot_li += li
+        tot_t += dt
+    value = tot_li / tot_t
+    sample = f"{len(cubes)} contiguous Morton-ordered cubes of {args.workload}, {args.cpu_iters} iterations per level, in-memory semantics, {threads} threads"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "cubes_sample": len(cubes), "iters_per_level": args.cpu_iters,
+                       "semantics": "tgv_minimize"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def measure_e2e(args, w, ctx, prm, mode, leaves, out_t, stream):
+    """The same solve through the public host-buffer call (tgvg_tgv_minimize):
+    cubes and histograms copied from pinned host memory, state copied back,
+    every step."""
+    import ctypes as C
+    import torch
+    from tgvreconclaude_gb300 import _native as N, api, formats as F
+    n, nbins = len(w.cubes), w.hists.shape[1]
+    pin_c = torch.from_numpy(w.cubes.view(np.int32).reshape(n, 4).copy()).pin_memory()
+    pin_h = torch.from_numpy(w.hists.view(np.int32).copy()).pin_memory()
+    pin_o = torch.empty((n, 13), dtype=torch.float32).pin_memory()
+    c_np = pin_c.numpy().view(F.CUBE_DTYPE).reshape(n)
+    h_np = pin_h.numpy().view(np.uint32)
+    o_np = pin_o.numpy().view(F.STATE_DTYPE).reshape(n)
+    lv = None if leaves is None else np.ascontiguousarray(leaves, F.LEAF_DTYPE)
+    p = prm.struct()
+    stt = N.Stats()
+    steps = max(1, min(args.steps, args.e2e_steps))
+
+    def call():
+        rc = ctx.lib.tgvg_tgv_minimize(ctx.h, c_np.ctypes.data, h_np.ctypes.data, n, nbins, api._p(lv),
+                                       0 if lv is None else len(lv), api.MODES[mode], C.byref(p), None,
+                                       o_np.ctypes.data, C.byref(stt))
+        ctx.check(rc, "tgvg_tgv_minimize")
+        return stt.leaf_iters
+
+    call()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    t_w = time.perf_counter()
+    li = sum(call() for _ in range(steps))
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_w
+    t = max(f0.elapsed_time(f1) / 1e3, 1e-9)
+    same = bool(np.array_equal(o_np.view(np.float32).reshape(n, 13), out_t.cpu().numpy()))
+    return {"value": li / t, "unit": UNIT, "h2d_bytes_per_step": int(16 * n + 4 * nbins * n),
+            "d2h_bytes_per_step": int(52 * n), "steps": steps, "wall_s": t_wall, "matches_device_run": same}
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    from tgvreconclaude_gb300 import _native as N, api, workloads, formats as F
+    t0 = time.time()
+    if args.cache and os.path.exists(args.cache):
+        w = workloads.load(args.cache)
+    else:
+        w = workloads.build(args.workload, seed=args.seed + rank, device="cuda", verbose=rank == 0,
+                            max_cubes=args.max_cubes or None)
+        if args.cache:
+            workloads.save(w, args.cache)
+    t_gen = time.time() - t0
+    torch.cuda.empty_cache()  # drop the generator's temporaries before timing
+    cfg = w.cfg
+    ctx = api.context()
+    n = len(w.cubes)
+    nbins = w.hists.shape[1]
+    cubes_t = torch.from_numpy(w.cubes.view(np.int32).reshape(n, 4)).cuda()
+    hists_t = torch.from_numpy(w.hists.view(np.int32)).cuda()
+    out_t = torch.empty((n, 13), dtype=torch.float32, device="cuda")
+    prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=args.iters or cfg["iters"])
+    mode = "stream" if cfg["chunks"] > 1 else "inmem"
+    leaves = w.leaves if mode == "stream" else None
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    for _ in range(args.warmup):
+        api.tgv_solve_device(cubes_t, hists_t, out_t, leaves, mode, prm)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    ctx.lib.tgvg_set_timing(ctx.h, 1)
+    clocks = Clocks(local)
+    clocks.start()
+    k0 = ctx.kernel_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    li, kt_d, kt_p, kt_n, kt_active = 0, 0.0, 0.0, 0, 0
+    for _ in range(args.steps):
+        st = api.tgv_solve_device(cubes_t, hists_t, out_t, leaves, mode, prm)
+        li += st["leaf_iters"]
+        kt_d += st["kt_dual_ms"]
+        kt_p += st["kt_primal_ms"]
+        kt_n += st["kt_launches"]
+        kt_active = st["kt_active"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.kernel_count() - k0
+    clk = clocks.stop()
+    ctx.lib.tgvg_set_timing(ctx.h, 0)
+    if pg:
+        pg.barrier()
+    elapsed = allreduce_max(e0.elapsed_time(e1) / 1e3, pg, torch)
+    li_all = allreduce_sum(li, pg, torch)
+    value = li_all / elapsed
+
+    # ---- roofline of the dominant iteration kernel (per launch, CUDA events)
+    hbm, peak_kind = peaks()
+    dual_ms, primal_ms = kt_d / max(1, kt_n), kt_p / max(1, kt_n)
+    dom, ms, bpc = ("k_dual", dual_ms, BYTES_DUAL) if kt_d >= kt_p else ("k_primal", primal_ms, BYTES_PRIMAL)
+    achieved = bpc * kt_active / (ms * 1e-3) / 1e9 if ms > 0 else None
+    tpc = traffic_per_cube().get(dom)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": (achieved / hbm) if achieved else None, "peak_kind": peak_kind,
+            "traffic": (tpc * kt_active) if tpc else None,
+            "bytes_per_launch": bpc * kt_active, "avg_launch_ms": ms, "active_cubes": kt_active,
+            "iteration_achieved": BYTES_ITER * kt_active / ((dual_ms + primal_ms) * 1e-3) / 1e9
+            if dual_ms + primal_ms > 0 else None,
+            "other_kernel_ms": primal_ms if dom == "k_dual" else dual_ms}
+
+    result = None
+    if rank == 0:
+        e2e = {} if args.skip_e2e else measure_e2e(args, w, ctx, prm, mode, leaves, out_t, stream)
+
+        # ---- Stage 5 on the same workload: pyramids + binning, host buffers in/out
+        hs = {}
+        if not args.skip_hist:
+            h_t0 = time.perf_counter()
+            hh = api.compute_histograms_from_maps(w.cubes, w.cams, w.depths, cfg["origin"], cfg["r_root"], nbins)
+            h_dt = time.perf_counter() - h_t0
+            pairs = n * len(w.cams)
+            hs = {"pairs_per_s_e2e": pairs / h_dt, "ms_e2e": 1e3 * h_dt, "pairs": pairs,
+                  "matches_workload": bool(np.array_equal(hh, w.hists))}
+
+        # ---- CPU oracle baseline on a bounded sample (1 thread)
+        cb = {}
+        if not args.skip_cpu:
+            cubes_s, hists_s = cpu_sample(w, args.cpu_sample, args.cpu_iters)
+            v, dt, lis = time_cpu_oracle(cubes_s, hists_s, args.cpu_iters, 1)
+            cb = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "seconds": dt, "host_cores": os.cpu_count(),
+                  "sample": f"{len(cubes_s)} contiguous Morton-ordered cubes of {args.workload}, {args.cpu_iters} iterations per "
+                            f"level, in-memory semantics, single thread"}
+
+        depth_hist = np.bincount(w.cubes["depth"], minlength=22)
+        result = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "cubes": n, "cameras": len(w.cams),
+                       "image": f"{cfg['width']}x{cfg['height']}", "max_depth": cfg["max_depth"], "nbins": nbins,
+                       "iters_per_level": prm.iters, "alpha1": prm.alpha1, "alpha0": prm.alpha0,
+                       "semantics": "tgv_minimize" if mode == "inmem" else "tgv_minimize_streaming (batched)",
+                       "chunks": len(w.leaves), "levels": {int(k): int(v) for k, v in enumerate(depth_hist) if v},
+                       "l2": "inputs larger than L2 (about 100 B of state per cube)",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "histograms": hs, "clocks": clk,
+            "gpu_launches": int(launches), "leaf_iters_per_step": int(li_all / args.steps),
+            "gen_s": round(t_gen, 1),
+        }
+        print(json.dumps(result), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="three64")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--iters", type=int, default=0, help="override iterations per level")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=1000000)
+    ap.add_argument("--cpu-iters", type=int, default=50)
+    ap.add_argument("--ref-sample", type=int, default=2000000)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-hist", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--max-cubes", type=int, default=0, help="truncate the workload (profiling runs)")
+    ap.add_argument("--cache", default="", help="load the workload from / save it to this .npz (profiling runs)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

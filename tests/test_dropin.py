@@ -1,0 +1,37 @@
+"""The C++ drop-in (tgvreconclaude_gb300/dropin/tgv_dropin.cpp) compiles against
+the reference's own headers and links into the reference's own Stage-5/6 test
+programs in place of src/histogram.cpp and src/tgv.cpp.  Needs the reference
+checkout; without a GPU the programs must stop at their first call with the
+no-device error (there is no CPU path)."""
+import os
+import subprocess
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DROPIN = os.path.join(REPO, "tgvreconclaude_gb300", "dropin")
+REF_DIR = os.environ.get("TGV_REFERENCE_DIR", "/root/reference")
+
+pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF_DIR, "tests")),
+                                reason="reference checkout absent")
+
+
+def test_dropin_links_reference_tests():
+    from tgvreconclaude_gb300 import _native
+    _native.build()
+    r = subprocess.run(["make", "-s", "-C", DROPIN, f"REF_DIR={REF_DIR}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for t in ("test_stage5_dropin", "test_stage6_dropin"):
+        assert os.path.exists(os.path.join(DROPIN, "_build", t))
+
+
+def test_dropin_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    exe = os.path.join(DROPIN, "_build", "test_stage6_dropin")
+    if not os.path.exists(exe):
+        test_dropin_links_reference_tests()
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode != 0
+    assert "no usable sm_103 device" in r.stderr

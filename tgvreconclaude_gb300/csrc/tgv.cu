@@ -30,6 +30,8 @@
 #include <cstring>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 
 namespace tgvg {
@@ -736,11 +738,14 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     std::vector<int> h_iters(nslot);
     std::vector<double> h_res(nslot);
     // optional per-launch timing of the largest level (not for sequential OC leaves)
-    int t_level = -1;
-    if (ctx->timing && mode != M_OC && iters > 0) {
+    int big_level = -1, t_level = -1;
+    {
         int best = 0;
         for (int Ld = min_d; Ld <= max_d; ++Ld)
-            if (h_bstart[Ld + 1] - h_bstart[Ld] > best) { best = h_bstart[Ld + 1] - h_bstart[Ld]; t_level = Ld; }
+            if (h_bstart[Ld + 1] - h_bstart[Ld] > best) { best = h_bstart[Ld + 1] - h_bstart[Ld]; big_level = Ld; }
+    }
+    if (ctx->timing && mode != M_OC && iters > 0) {
+        t_level = big_level;
         while ((int)ctx->tev.size() < 3 * iters) {
             cudaEvent_t e;
             TGVG_CK(ctx, cudaEventCreate(&e));
@@ -780,6 +785,8 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                                          ctx->stream));
             TGVG_CK(ctx, cudaMemsetAsync(resid, 0, 8ull * nslot, ctx->stream));
         }
+        // NVTX range per level so profilers can select the largest level's launches
+        nvtxRangePushA(Ld == big_level ? "tgv_largest_level" : "tgv_level");
         for (const Unit& u : us) {
             IterArgs a;
             a.o = u.o; a.n = u.n; a.npos = n;
@@ -810,6 +817,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                 }
             }
         }
+        nvtxRangePop();
         // level stats
         if (st.n_levels < TGVG_MAX_LEVELS) {
             const int k = st.n_levels++;

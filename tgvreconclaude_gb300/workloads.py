@@ -26,7 +26,7 @@ from . import _native as N, formats as F, scenes as S
 CONFIGS = {
     "torus16": dict(scene="torus", ncam=16, cam_radius=3.0, width=640, height=480, half_fov=25.0,
                     origin=(-1.5, -1.5, -1.5), r_root=1.5, max_depth=8, nbins=10, iters=300, chunks=1),
-    "three64": dict(scene="three", ncam=64, cam_radius=7.0, width=1920, height=1080, half_fov=25.0,
+    "three64": dict(scene="three", ncam=64, cam_radius=4.5, width=1920, height=1080, half_fov=25.0,
                     origin=(-3.0, -3.0, -3.0), r_root=3.0, max_depth=11, nbins=10, iters=1000, chunks=1),
     "terrain128": dict(scene="terrain", ncam=128, cam_radius=4.0, width=1280, height=960, half_fov=30.0,
                        origin=(-4.0, -4.0, -4.0), r_root=4.0, max_depth=12, nbins=10, iters=1000, chunks=64),
@@ -102,9 +102,21 @@ def chunk_leaves(cubes, k: int, rng, lo=50_000, hi=4_000_000):
     return leaves
 
 
+def save(w: Workload, path: str) -> None:
+    """Cubes, histograms and leaves of a workload (no depth maps) as one .npz."""
+    np.savez(path, name=w.name, cubes=w.cubes, hists=w.hists, leaves=w.leaves)
+
+
+def load(path: str) -> Workload:
+    d = np.load(path)
+    name = str(d["name"])
+    return Workload(name, dict(CONFIGS[name]), [], None, d["cubes"], d["hists"], d["leaves"], {})
+
+
 def build(name: str, seed: int = 0, device: str = "cuda", keep_depths: bool = False,
-          max_cubes: int | None = None, verbose: bool = False) -> Workload:
-    """Generate workload `name` (see module docstring)."""
+          max_cubes: int | None = None, verbose: bool = False, histograms: bool = True) -> Workload:
+    """Generate workload `name` (see module docstring).  With histograms=False
+    the histogram rows are left empty for the caller to fill."""
     import torch
     from . import api
     cfg = dict(CONFIGS[name])
@@ -133,7 +145,10 @@ def build(name: str, seed: int = 0, device: str = "cuda", keep_depths: bool = Fa
     if max_cubes and len(cubes) > max_cubes:
         cubes = cubes[:max_cubes]
     t2 = time.time()
-    hists = api.compute_histograms_from_maps(cubes, cams, depths, cfg["origin"], cfg["r_root"], cfg["nbins"])
+    if histograms:
+        hists = api.compute_histograms_from_maps(cubes, cams, depths, cfg["origin"], cfg["r_root"], cfg["nbins"])
+    else:
+        hists = np.zeros((len(cubes), cfg["nbins"]), np.uint32)
     t3 = time.time()
     leaves = chunk_leaves(cubes, cfg["chunks"], rng)
     w = Workload(name, cfg, cams, depths if keep_depths else None, cubes, hists, leaves,
