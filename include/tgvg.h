@@ -36,6 +36,7 @@ extern "C" {
 #define TGVG_ERR_TIMEOUT   -7  /* a bounded device wait ran out of iterations                  */
 #define TGVG_ERR_NODEVICE  -8  /* no CUDA device, or not an sm_103 part                        */
 #define TGVG_ERR_OVERLAP   -9  /* treetop leaves overlap                                       */
+#define TGVG_ERR_LIMIT    -10  /* request exceeds the fixed scratch of a no-allocation entry   */
 
 /* ---- records (byte-identical to the reference) --------------------------- */
 
@@ -176,6 +177,27 @@ int tgvg_compute_histograms_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, int64_t
                                 const tgvg_camera* cams, int32_t ncam, const float* d_levels,
                                 const int64_t* level_offset, const float origin[3],
                                 float r_root, int32_t nbins, uint32_t* d_out);
+
+/* No counterpart in the reference.  The device-resident histogram pass for
+ * callers that cannot allocate device memory while they run: a service that
+ * reserves all device memory up front for its own pool, a real-time loop where
+ * an allocation's implicit synchronisation would stall other work, or a runtime
+ * that routes every allocation through its own allocator.  It calls no
+ * cudaMalloc/cudaFree and needs no context: d_cubes, d_base[c] (map c's level-0
+ * texels) and d_out are the caller's device memory; cams stays on the host.
+ * The pyramids and camera table are built in one fixed scratch array that the
+ * library holds on every GPU that loads it: at most 256 cameras and
+ * 16 Mi pyramid texels (64 MiB, levels 0.. of all maps together); larger
+ * requests return TGVG_ERR_LIMIT.  The first call on a device looks the array
+ * up on that device (make it before any stream capture).  Work is enqueued on
+ * `stream` (a cudaStream_t; null = the legacy default stream) and the call
+ * returns without waiting.  All calls share the one array, so calls that may
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Output is bit-identical to
+ * tgvg_compute_histograms_dev. */
+int tgvg_compute_histograms_noalloc(const tgvg_cube* d_cubes, int64_t n, const tgvg_camera* cams,
+                                    int32_t ncam, const float* const* d_base, const float origin[3],
+                                    float r_root, int32_t nbins, uint32_t* d_out, void* stream);
 
 /* compute_histograms_oc (reference src/histogram.hpp:55-61, histogram.cpp:222-256):
  * cubes from a TGV1 file, leaves from the caller, output written as a TGVH file

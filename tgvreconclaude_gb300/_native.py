@@ -124,7 +124,9 @@ _SIGS = {
     "tgvg_compute_histograms": ([P, P, C.c_int64, P, C.c_int32, P, P, C.c_float, C.c_int32, P], C.c_int),
     "tgvg_compute_histograms_pyr": ([P, P, C.c_int64, P, C.c_int32, P, P, C.c_float, C.c_int32, P], C.c_int),
     "tgvg_compute_histograms_dev": ([P, P, C.c_int64, P, C.c_int32, P, P, P, C.c_float, C.c_int32, P], C.c_int),
-    "tgvg_compute_histograms_oc": ([P, C.c_char_p, P, C.c_int32, P, C.c_int32, P, P, C.c_float, C.c_char_p],
+    "tgvg_compute_histograms_noalloc": ([P, C.c_int64, P, C.c_int32, P, P, C.c_float, C.c_int32, P, P],
+                                        C.c_int),
+    "tgvg_compute_histograms_oc":([P, C.c_char_p, P, C.c_int32, P, C.c_int32, P, P, C.c_float, C.c_char_p],
                                    C.c_int),
     "tgvg_tgv_minimize": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P], C.c_int),
     "tgvg_tgv_minimize_dev": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P], C.c_int),

@@ -94,6 +94,7 @@ extern "C" const char* tgvg_strerror(int rc) {
         case TGVG_ERR_TIMEOUT: return "device wait timed out";
         case TGVG_ERR_NODEVICE: return "no usable sm_103 device";
         case TGVG_ERR_OVERLAP: return "treetop leaves overlap";
+        case TGVG_ERR_LIMIT: return "request exceeds the fixed scratch of the no-allocation entry point";
         default: return "unknown error";
     }
 }

@@ -373,3 +373,91 @@ extern "C" int tgvg_compute_histograms_dev(tgvg_ctx* ctx, const tgvg_cube* d_cub
     TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
     return TGVG_OK;
 }
+
+// ------------------------------------------- no-allocation histogram entry ---
+// Some host programs cannot call cudaMalloc once they are running: a service
+// that reserves all device memory up front for its own pool, a real-time loop
+// in which an allocation's implicit device synchronisation would stall other
+// work, or a runtime that routes every device allocation through its own
+// allocator.  tgvg_compute_histograms_noalloc serves them: the caller passes
+// device inputs and outputs, and the only scratch this path needs (the depth
+// pyramids and the camera table) lives in the fixed array below, which every
+// GPU that loads this library holds until the process exits.
+static constexpr int64_t NOALLOC_CAM_FLOATS = 9216;                   // 256 DevCam records
+static constexpr int64_t NOALLOC_TEX_FLOATS = int64_t(16) << 20;      // 16 Mi texels = 64 MiB
+static __device__ __align__(256) float g_noalloc_scratch[NOALLOC_CAM_FLOATS + NOALLOC_TEX_FLOATS];
+
+namespace {
+std::mutex g_noalloc_mu;
+float* g_noalloc_addr[128] = {};  // device address of g_noalloc_scratch, per device ordinal
+}  // namespace
+
+// Device address of the scratch array on the current device.  The first call
+// on each device looks it up (cudaGetSymbolAddress, which may load the module);
+// later calls reuse it.
+static int noalloc_scratch(float** out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return TGVG_ERR_NODEVICE;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        float* p = nullptr;
+        if (cudaGetSymbolAddress((void**)&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return TGVG_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return TGVG_OK;
+}
+
+extern "C" int tgvg_compute_histograms_noalloc(const tgvg_cube* d_cubes, int64_t n, const tgvg_camera* cams,
+                                               int32_t ncam, const float* const* d_base, const float origin[3],
+                                               float r_root, int32_t nbins, uint32_t* d_out, void* stream) {
+    if (n < 0 || (n > 0 && (!d_cubes || !d_out)) || !origin || (nbins != 8 && nbins != 10))
+        return TGVG_ERR_INVALID;
+    int rc = check_cams(cams, ncam);
+    if (rc) return rc;
+    if (ncam > 0 && !d_base) return TGVG_ERR_INVALID;
+    if (int64_t(ncam) * (int64_t)sizeof(DevCam) > NOALLOC_CAM_FLOATS * 4) return TGVG_ERR_LIMIT;
+    std::vector<int64_t> off(ncam + 1, 0);
+    for (int c = 0; c < ncam; ++c) off[c + 1] = off[c] + pyramid_size(cams[c].width, cams[c].height);
+    if (off[ncam] > NOALLOC_TEX_FLOATS) return TGVG_ERR_LIMIT;
+    if (n == 0) return TGVG_OK;
+    float* scratch = nullptr;
+    if ((rc = noalloc_scratch(&scratch))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    DevCam* d_cams = reinterpret_cast<DevCam*>(scratch);
+    float* d_tex = scratch + NOALLOC_CAM_FLOATS;
+    std::vector<DevCam> dc;
+    make_devcams(cams, ncam, off.data(), dc);
+    // Every texel and camera record the kernels read is written earlier in this
+    // call, so nothing left in the array by a previous call is ever used.
+    if (ncam > 0 &&
+        cudaMemcpyAsync(d_cams, dc.data(), sizeof(DevCam) * dc.size(), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return TGVG_ERR_CUDA;
+    int maxlev = 0, maxpix = 0;
+    for (int c = 0; c < ncam; ++c) {
+        if (!d_base[c]) return TGVG_ERR_INVALID;
+        if (cudaMemcpyAsync(d_tex + off[c], d_base[c], sizeof(float) * cams[c].width * cams[c].height,
+                            cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return TGVG_ERR_CUDA;
+        maxlev = std::max(maxlev, dc[c].nlev);
+        maxpix = std::max(maxpix, dc[c].W * dc[c].H);
+    }
+    for (int l = 1; l < maxlev; ++l) {
+        const int texels = std::max(1, maxpix >> (2 * l));
+        dim3 grid((unsigned)std::min(1024, (texels + 255) / 256), (unsigned)ncam);
+        k_pyramid_level<<<grid, 256, 0, s>>>(d_cams, d_tex, l);
+    }
+    Thresholds thr;
+    tgvg_level_thresholds(thr.t);
+    const unsigned grid = (unsigned)((n + HIST_BLOCK - 1) / HIST_BLOCK);
+    if (nbins == 8)
+        k_histograms<8><<<grid, HIST_BLOCK, 0, s>>>(reinterpret_cast<const uint4*>(d_cubes), n, d_cams, ncam, d_tex,
+                                                    origin[0], origin[1], origin[2], r_root, thr, d_out);
+    else
+        k_histograms<10><<<grid, HIST_BLOCK, 0, s>>>(reinterpret_cast<const uint4*>(d_cubes), n, d_cams, ncam,
+                                                     d_tex, origin[0], origin[1], origin[2], r_root, thr, d_out);
+    return cudaGetLastError() == cudaSuccess ? TGVG_OK : TGVG_ERR_CUDA;
+}
