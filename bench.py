@@ -297,6 +297,7 @@ def run_ours(args):
         kt_p += st["kt_primal_ms"]
         kt_n += st["kt_launches"]
         kt_active = st["kt_active"]
+        last_st = st
     e1.record(stream)
     torch.cuda.synchronize()
     launches = ctx.kernel_count() - k0
@@ -359,6 +360,9 @@ def run_ours(args):
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "histograms": hs, "clocks": clk,
             "gpu_launches": int(launches), "leaf_iters_per_step": int(li_all / args.steps),
+            "levels_detail": [{"depth": d, "active": int(a), "ms": round(m, 3), "schedule": s}
+                              for d, a, m, s in zip(last_st["depth"], last_st["active"], last_st["level_ms"],
+                                                    last_st["schedule"])],
             "gen_s": round(t_gen, 1),
         }
         print(json.dumps(result), flush=True)

@@ -84,6 +84,9 @@ typedef struct tgvg_params {
     int32_t init;            /* TGVG_INIT_*                                             */
     float tol;               /* relative residual stop; 0 = fixed count (reference)     */
     int32_t check_every;     /* residual evaluated every this many iterations           */
+    int32_t keep_init_u;     /* 0 (reference): a level's cubes copy u and v from their  */
+                             /* parent; 1: they keep their initial u and copy only v     */
+                             /* (a warm start or a literal zero start at every level)   */
 } tgvg_params;
 
 #define TGVG_INIT_MEDIAN 0   /* u = median_indicator (reference, tgv.cpp:372-373) */
@@ -115,6 +118,8 @@ typedef struct tgvg_stats {
     int32_t kt_launches;
     int64_t kt_active;
     double kt_dual_ms, kt_primal_ms;
+    double level_ms[TGVG_MAX_LEVELS];    /* device time of level slot k (init + iterations) */
+    int32_t schedule[TGVG_MAX_LEVELS];   /* iteration schedule used for level slot k       */
 } tgvg_stats;
 
 typedef struct tgvg_ctx tgvg_ctx;
@@ -140,6 +145,12 @@ void tgvg_level_thresholds(float* t13);
 /* Turn per-launch event timing of the largest level's iteration kernels on (1)
  * or off (0); results land in tgvg_stats.kt_*. */
 int tgvg_set_timing(tgvg_ctx* ctx, int on);
+/* Iteration schedule of a level whose active count n has floor(log2 n) == cls
+ * (cls = -1: every class), for one mode: 0 = two launches per iteration, 1..6 =
+ * one cooperative launch per level with about 256 << k cubes per block, 7 = as 0
+ * with the sweep kernels capped at 32 registers, -1 = let the online autotuner
+ * choose (default).  Results do not depend on it. */
+int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
 
 /* ---- Stage 5: depth maps -> histograms ------------------------------------ */
 

@@ -49,7 +49,8 @@ class Camera(C.Structure):
 
 class Params(C.Structure):
     _fields_ = [("alpha0", C.c_float), ("alpha1", C.c_float), ("iters", C.c_int32),
-                ("init", C.c_int32), ("tol", C.c_float), ("check_every", C.c_int32)]
+                ("init", C.c_int32), ("tol", C.c_float), ("check_every", C.c_int32),
+                ("keep_init_u", C.c_int32)]
 
 
 class LevelStats(C.Structure):
@@ -179,9 +180,10 @@ INITS = {"median": 0, "zero": 1, "given": 2}
 
 
 def tgv_solve(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04, iters=200,
-              init="median", u_init=None, tol=0.0, check_every=10, fp64=False, nthreads=1):
+              init="median", u_init=None, tol=0.0, check_every=10, fp64=False, nthreads=1, keep_init_u=False):
     """Oracle solve.  Returns (state, level_stats).  State is a STATE_DTYPE array
-    (float) or an (n, 13) float64 array when fp64."""
+    (float) or an (n, 13) float64 array when fp64.  keep_init_u: levels keep
+    their initial u and copy only v from the parent (warm / zero start)."""
     cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
     hists = np.ascontiguousarray(hists, np.uint32)
     n = len(cubes)
@@ -193,7 +195,7 @@ def tgv_solve(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04,
         if n == 0:
             leaves = np.zeros(0, LEAF_DTYPE)
     leaves = np.ascontiguousarray(leaves, LEAF_DTYPE)
-    p = Params(alpha0, alpha1, iters, INITS[init], tol, check_every)
+    p = Params(alpha0, alpha1, iters, INITS[init], tol, check_every, int(keep_init_u))
     ui = None if u_init is None else np.ascontiguousarray(u_init, np.float32)
     ls = (LevelStats * 24)()
     nls = C.c_int()
@@ -209,6 +211,33 @@ def tgv_solve(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04,
     stats = [dict(depth=ls[i].depth, iters_run=ls[i].iters_run, active=ls[i].active,
                   residual=ls[i].residual) for i in range(nls.value)]
     return out, stats
+
+
+def stream_init(cubes, hists):
+    """Initial streaming state: u = median_indicator (float, reference order), rest 0."""
+    h = np.ascontiguousarray(hists, np.uint32)
+    nb = h.shape[1]
+    tot = h.sum(1, dtype=np.uint32)
+    cum = np.cumsum(h, 1, dtype=np.uint32)
+    k = np.argmax(cum * np.uint32(2) >= tot[:, None], axis=1)
+    med = np.float32(-1.0) + (k.astype(np.float32) + np.float32(0.5)) / np.float32(nb / 2.0)
+    st = np.zeros(len(cubes), STATE_DTYPE)
+    st["u"] = np.where(tot > 0, med, np.float32(0.0))
+    return st
+
+
+def stream_level(cubes, hists, leaves, mask, level, params, state, nthreads=1):
+    """One rank's share of one streaming level (orc_stream_level), in place.
+    params: dict(alpha0, alpha1, iters)."""
+    cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    hists = np.ascontiguousarray(hists, np.uint32)
+    leaves = np.ascontiguousarray(leaves, LEAF_DTYPE)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    p = Params(params["alpha0"], params["alpha1"], params["iters"], 0, 0.0, 1)
+    assert state.flags["C_CONTIGUOUS"] and state.dtype == STATE_DTYPE
+    rc = lib().orc_stream_level(_ptr(cubes), _ptr(hists), C.c_int64(len(cubes)), hists.shape[1], _ptr(leaves),
+                                len(leaves), _ptr(mask), level, C.byref(p), _ptr(state), nthreads)
+    assert rc == 0
 
 
 # ------------------------------------------------------ reference (libref) ---

@@ -431,6 +431,13 @@ struct Problem {
     S tol;
     int check_every;
     int nthreads;
+    // Sharded streaming (one rank's share of one level): iterate only the
+    // leaves with a nonzero mask entry, run only level `only_level`, start from
+    // `state_in` instead of the initial state.
+    const uint8_t* leaf_mask = nullptr;
+    int only_level = -1;
+    const State* state_in = nullptr;
+    int keep_init_u = 0;  // extension: parent init copies only v (warm / zero start per level)
 };
 
 // Reference binary search over the Morton-sorted cube array: returns the first
@@ -458,6 +465,12 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
         st[i] = St<S>{};
         if (P.init == 0) st[i].u = dt[i].has ? dt[i].med : S(0);  // median_indicator
         else if (P.init == 2) st[i].u = S(P.u_init[i]);
+        if (P.state_in) {
+            const State& s = P.state_in[i];
+            st[i].u = S(s.u);
+            for (int c = 0; c < 3; ++c) { st[i].v[c] = S(s.v[c]); st[i].p[c] = S(s.p[c]); }
+            for (int c = 0; c < 6; ++c) st[i].q[c] = S(s.q[c]);
+        }
     }
     int nls = 0;
     if (N == 0) { if (n_lstats) *n_lstats = 0; return 0; }
@@ -497,7 +510,7 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
                 for (uint32_t i : all) {
                     int32_t pi = find(parent_key(keys[i], L));
                     if (pi >= 0) {
-                        st[i].u = st[pi].u;
+                        if (!P.keep_init_u) st[i].u = st[pi].u;
                         for (int c = 0; c < 3; ++c) st[i].v[c] = st[pi].v[c];
                     }
                     for (int c = 0; c < 3; ++c) st[i].p[c] = S(0);
@@ -549,6 +562,7 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
             return true;
         };
         for (int L = min_d; L <= max_d; ++L) {
+            if (P.only_level >= 0 && L != P.only_level) continue;
             if (L > min_d) {  // parent init, leaf by leaf (tgv.cpp:878-934)
                 for (int l = 0; l < P.nleaf; ++l) {
                     uint32_t f0, nl;
@@ -558,7 +572,7 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
                         if (P.cubes[i].depth != L) continue;
                         uint32_t g = file_lookup(keys, parent_key(keys[i], L));
                         if (g != 0xffffffffu) {
-                            st[i].u = st[g].u;
+                            if (!P.keep_init_u) st[i].u = st[g].u;
                             for (int c = 0; c < 3; ++c) st[i].v[c] = st[g].v[c];
                         }
                         for (int c = 0; c < 3; ++c) st[i].p[c] = S(0);
@@ -576,6 +590,7 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
             for (int l = 0; l < P.nleaf; ++l) {
                 uint32_t f0, nl;
                 if (!leaf_range(l, f0, nl)) continue;
+                if (P.leaf_mask && !P.leaf_mask[l]) continue;  // another rank's leaf
                 std::vector<uint32_t> act;
                 for (uint32_t li = 0; li < nl; ++li)
                     if (P.cubes[f0 + li].depth == L) act.push_back(li);
@@ -673,6 +688,7 @@ struct orc_params {
     int32_t init;         // 0 median (reference), 1 zero, 2 caller u
     float tol;            // 0: fixed iteration count (reference behaviour)
     int32_t check_every;  // residual period when tol > 0
+    int32_t keep_init_u;  // 1: levels keep their initial u, copy only v from the parent
 };
 
 int orc_abi_version() { return 1; }
@@ -719,10 +735,12 @@ static int solve_f32(const orc::Cube* cubes, const uint32_t* hists, int64_t n, i
     if (nbins == 8) {
         orc::Problem<float, 8> P{cubes, n, hists, leaves, nleaf, mode, p->alpha0, p->alpha1, p->iters,
                                  p->init, u_init, p->tol, p->check_every, nthreads};
+        P.keep_init_u = p->keep_init_u;
         rc = orc::solve<float, 8>(P, s.data(), ls, nls);
     } else if (nbins == 10) {
         orc::Problem<float, 10> P{cubes, n, hists, leaves, nleaf, mode, p->alpha0, p->alpha1, p->iters,
                                   p->init, u_init, p->tol, p->check_every, nthreads};
+        P.keep_init_u = p->keep_init_u;
         rc = orc::solve<float, 10>(P, s.data(), ls, nls);
     } else {
         return -1;
@@ -752,11 +770,13 @@ int orc_tgv_solve_f64(const orc::Cube* cubes, const uint32_t* hists, int64_t n, 
         orc::Problem<double, 8> P{cubes, n, hists, leaves, nleaf, mode, double(p->alpha0),
                                   double(p->alpha1), p->iters, p->init, u_init, double(p->tol),
                                   p->check_every, nthreads};
+        P.keep_init_u = p->keep_init_u;
         rc = orc::solve<double, 8>(P, s.data(), ls, nls);
     } else if (nbins == 10) {
         orc::Problem<double, 10> P{cubes, n, hists, leaves, nleaf, mode, double(p->alpha0),
                                    double(p->alpha1), p->iters, p->init, u_init, double(p->tol),
                                    p->check_every, nthreads};
+        P.keep_init_u = p->keep_init_u;
         rc = orc::solve<double, 10>(P, s.data(), ls, nls);
     } else {
         return -1;
@@ -792,5 +812,34 @@ int64_t orc_check_thresholds(const float* t) {
     for (float x : big)
         if (std::min(12, orc::trunc_i32(std::log2(x))) != lvl(x)) ++bad;
     return bad;
+}
+}
+
+extern "C" {
+// One rank's share of one level of the streaming semantics: parent init of
+// every leaf's level-L cubes, the level-start snapshot of every cube, then
+// iterations of the leaves whose mask entry is nonzero.  `state` (n TGVCube
+// records) is read as the state before the level and overwritten with the
+// state after it.  Float, fixed iteration count.
+int orc_stream_level(const orc::Cube* cubes, const uint32_t* hists, int64_t n, int nbins,
+                     const orc::Leaf* leaves, int nleaf, const uint8_t* leaf_mask, int level,
+                     const orc_params* p, orc::State* state, int nthreads) {
+    std::vector<orc::St<float>> s(static_cast<size_t>(n));
+    int rc;
+    if (nbins == 8) {
+        orc::Problem<float, 8> P{cubes, n, hists, leaves, nleaf, orc::STREAM, p->alpha0, p->alpha1, p->iters,
+                                 0, nullptr, 0.0f, 1, nthreads};
+        P.leaf_mask = leaf_mask; P.only_level = level; P.state_in = state;
+        rc = orc::solve<float, 8>(P, s.data(), nullptr, nullptr);
+    } else if (nbins == 10) {
+        orc::Problem<float, 10> P{cubes, n, hists, leaves, nleaf, orc::STREAM, p->alpha0, p->alpha1, p->iters,
+                                  0, nullptr, 0.0f, 1, nthreads};
+        P.leaf_mask = leaf_mask; P.only_level = level; P.state_in = state;
+        rc = orc::solve<float, 10>(P, s.data(), nullptr, nullptr);
+    } else {
+        return -1;
+    }
+    std::memcpy(state, s.data(), sizeof(orc::State) * size_t(n));
+    return rc;
 }
 }

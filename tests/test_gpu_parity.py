@@ -169,6 +169,21 @@ def test_tgv_random_vs_oracle(oracle_lib, seed):
         assert_state_equal(out, ref, f"seed {seed} {mode}")
 
 
+def test_tgv_autotuned_schedules_are_exact(oracle_lib):
+    """300 iterations: the first solve tunes each level's schedule online
+    (per-sweep launches vs one cooperative launch per level, several grid
+    sizes), the second reuses the tuned table; both stay bit-identical."""
+    rng = np.random.default_rng(77)
+    cubes = S.random_octree(rng, dmin=1, dmax=7, target=60000, shape="sphere")
+    hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.05)
+    leaves = S.split_leaves(len(cubes), 5, rng, cubes, aligned=True)
+    for mode in ("inmem", "stream"):
+        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, alpha0=2.0, alpha1=1.0, iters=300, nthreads=8)
+        for _ in range(2):
+            out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=300))
+            assert_state_equal(out, ref, f"autotuned {mode}")
+
+
 def test_tgv_unsorted_inmem_and_leaf_gaps(oracle_lib):
     """In-memory semantics need no ordering; leaves may leave cubes uncovered."""
     rng = np.random.default_rng(9)

@@ -82,7 +82,7 @@ class Camera(C.Structure):
 
 class Params(C.Structure):
     _fields_ = [("alpha0", C.c_float), ("alpha1", C.c_float), ("iters", C.c_int32), ("init", C.c_int32),
-                ("tol", C.c_float), ("check_every", C.c_int32)]
+                ("tol", C.c_float), ("check_every", C.c_int32), ("keep_init_u", C.c_int32)]
 
 
 MAX_LEVELS = 22
@@ -95,7 +95,8 @@ class Stats(C.Structure):
                 ("leaf_iters", C.c_int64), ("kernel_launches", C.c_int32), ("reserved", C.c_int32),
                 ("setup_ms", C.c_double), ("iterate_ms", C.c_double), ("total_ms", C.c_double),
                 ("kt_depth", C.c_int32), ("kt_launches", C.c_int32), ("kt_active", C.c_int64),
-                ("kt_dual_ms", C.c_double), ("kt_primal_ms", C.c_double)]
+                ("kt_dual_ms", C.c_double), ("kt_primal_ms", C.c_double),
+                ("level_ms", C.c_double * MAX_LEVELS), ("schedule", C.c_int32 * MAX_LEVELS)]
 
     def as_dict(self):
         k = self.n_levels
@@ -105,7 +106,8 @@ class Stats(C.Structure):
                     leaf_iters=self.leaf_iters, kernel_launches=self.kernel_launches,
                     setup_ms=self.setup_ms, iterate_ms=self.iterate_ms, total_ms=self.total_ms,
                     kt_depth=self.kt_depth, kt_launches=self.kt_launches, kt_active=self.kt_active,
-                    kt_dual_ms=self.kt_dual_ms, kt_primal_ms=self.kt_primal_ms)
+                    kt_dual_ms=self.kt_dual_ms, kt_primal_ms=self.kt_primal_ms,
+                    level_ms=list(self.level_ms[:k]), schedule=list(self.schedule[:k]))
 
 
 P = C.c_void_p
@@ -119,6 +121,7 @@ _SIGS = {
     "tgvg_kernel_count": ([P], C.c_int64),
     "tgvg_level_thresholds": ([P], None),
     "tgvg_set_timing": ([P, C.c_int], C.c_int),
+    "tgvg_set_schedule": ([P, C.c_int32, C.c_int32, C.c_int32], C.c_int),
     "tgvg_pyramid_dims": ([C.c_int32, C.c_int32, P], C.c_int),
     "tgvg_build_pyramids": ([P, P, C.c_int32, P, P], C.c_int),
     "tgvg_compute_histograms": ([P, P, C.c_int64, P, C.c_int32, P, P, C.c_float, C.c_int32, P], C.c_int),

@@ -245,10 +245,11 @@ class TGVParams:
     init: str = "median"       # "median" (reference), "zero", "given"
     tol: float = 0.0           # relative residual stop; 0 = fixed iteration count
     check_every: int = 10
+    keep_init_u: bool = False  # True: every level keeps its initial u (warm / zero start), copies only v
 
     def struct(self) -> N.Params:
         return N.Params(self.alpha0, self.alpha1, self.iters, {"median": 0, "zero": 1, "given": 2}[self.init],
-                        self.tol, self.check_every)
+                        self.tol, self.check_every, int(self.keep_init_u))
 
 
 MODES = {"inmem": 0, "oc": 1, "stream": 2}

@@ -75,6 +75,14 @@ extern "C" void tgvg_level_thresholds(float* t13) {
     if (t13) level_thresholds(t13);
 }
 
+extern "C" int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg) {
+    if (!ctx || mode < 0 || mode > 2 || cls < -1 || cls > 31 || cfg < -1 || cfg > 7) return TGVG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    for (int c = 0; c < 32; ++c)
+        if (cls < 0 || c == cls) ctx->tune[mode][c] = cfg;
+    return TGVG_OK;
+}
+
 extern "C" int tgvg_set_timing(tgvg_ctx* ctx, int on) {
     if (!ctx) return TGVG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -125,6 +133,7 @@ extern "C" int tgvg_create(int device, tgvg_ctx** out) {
         return TGVG_ERR_CUDA;
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
+    for (auto& e : c->lev_ev) cudaEventCreate(&e);
     level_thresholds(c->lvl_thresh);
     *out = c;
     return TGVG_OK;
@@ -140,6 +149,7 @@ extern "C" int tgvg_destroy(tgvg_ctx* ctx) {
             if (b.p) cudaFree(b.p);
         for (auto& e : ctx->ev) cudaEventDestroy(e);
         for (auto& e : ctx->tev) cudaEventDestroy(e);
+        for (auto& e : ctx->lev_ev) cudaEventDestroy(e);
         cudaStreamDestroy(ctx->stream);
     }
     delete ctx;

@@ -152,6 +152,14 @@ struct tgvg_ctx {
     cudaEvent_t ev[4] = {};
     bool timing = false;               // per-launch events on the largest level
     std::vector<cudaEvent_t> tev;      // pool for those events
+    int tune[3][32];                   // chosen iteration schedule per mode and log2(size) class, -1 = untuned
+    int coop_max[3][2] = {};           // co-resident blocks of the persistent kernel per mode / stop
+    int iter_occ[3][2][2] = {};        // blocks/SM of the sweep kernels [mode][register-capped][dual, primal]
+    cudaEvent_t lev_ev[2 * TGVG_MAX_LEVELS] = {};  // per-level start/end
+    tgvg_ctx() {
+        for (auto& m : tune)
+            for (int& c : m) c = -1;
+    }
 
     // Device buffer `id` with room for `bytes` (grow-only; contents are not kept
     // across growth).  Returns nullptr after recording the error.

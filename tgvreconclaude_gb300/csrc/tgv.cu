@@ -291,7 +291,7 @@ __global__ void k_leaf_ranges(int nleaf, const int* __restrict__ leaf_first, con
 
 // ------------------------------------------------------------- per level ---
 
-__global__ void k_parent_init(int o, int n, const int* __restrict__ par, float4* __restrict__ uv,
+__global__ void k_parent_init(int o, int n, const int* __restrict__ par, int keep_u, float4* __restrict__ uv,
                               float4* __restrict__ bar, float4* __restrict__ P4, float4* __restrict__ Q4,
                               float* __restrict__ Q1) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -301,7 +301,11 @@ __global__ void k_parent_init(int o, int n, const int* __restrict__ par, float4*
     float4 s = uv[p];
     // A parent at this same level is a cube whose own parent lookup returns
     // itself, so it never changes here and can be read concurrently.
-    if (j >= 0 && j != p) { s = uv[j]; uv[p] = s; }
+    if (j >= 0 && j != p) {
+        const float4 q = uv[j];
+        s = keep_u ? make_float4(s.x, q.y, q.z, q.w) : q;  // keep_u: warm start keeps its own u
+        uv[p] = s;
+    }
     bar[p] = s;
     P4[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     Q4[p] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -336,9 +340,17 @@ struct IterArgs {
     const float4* snap;
     const int* lid;     // STREAM: stop/residual slot per position
     double* acc;        // [slot][4]: d_primal, d_dual, n_primal, n_dual
-    const int* done;    // [slot]
+    int* done;          // [slot]
     int slot0;          // INMEM/OC: the slot of this launch
     float alpha0, alpha1;
+    // persistent (one launch per level) schedule only
+    int iters, check_every, nslot, it0, iters_total;
+    float tol;
+    unsigned* bar_count;  // grid barrier state
+    unsigned* bar_gen;
+    int* err;             // set when a bounded wait gives up
+    int* iters_run;
+    double* resid;
 };
 
 // Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
@@ -390,141 +402,231 @@ __device__ __forceinline__ void clip6(float* q, float r) {
     }
 }
 
-template <int MODE>
+// Loads of state that other blocks rewrite while a persistent kernel runs go
+// to L2 (.cg) so no stale L1 line is ever read; the per-launch kernels use
+// ordinary loads.
+template <bool CG> __device__ __forceinline__ float4 ld4(const float4* p) { return CG ? __ldcg(p) : *p; }
+template <bool CG> __device__ __forceinline__ float ld1(const float* p) { return CG ? __ldcg(p) : *p; }
+
+template <int MODE, bool CG>
 __device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const float4* __restrict__ bar,
                                             const float4* __restrict__ snap) {
     if (j < 0) return own;
     if (MODE != M_INMEM && (j & BORDER)) return snap[j & POS_MASK];
-    return bar[j];
+    return ld4<CG>(bar + j);
 }
 
-// K6: dual ascent on p (|grad u - v|, radius alpha1) and q (|e(v)|, radius alpha0).
-template <int MODE, bool RES, bool STOP>
-__global__ void __launch_bounds__(ITER_BLOCK) k_dual(IterArgs a) {
-    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int beg = a.o + blockIdx.x * a.chunk;
-    const int end = min(a.o + a.n, beg + a.chunk);
-    WarpAcc wa;
-    for (int g = beg + warp * 32; g < end; g += ITER_BLOCK) {
-        const int p = g + lane;
-        int slot = -1;
-        if (p < end) slot = (MODE == M_STREAM) ? a.lid[p] : a.slot0;
-        bool work = p < end;
-        if (STOP && work && MODE == M_STREAM) work = !a.done[slot];
-        double dd = 0.0, nd = 0.0;
-        if (work) {
-            const float4 b = a.bar[p];
-            const int j0 = a.nb[p], j2 = a.nb[2 * a.npos + p], j4 = a.nb[4 * a.npos + p];
-            const float4 B0 = fetch_bar<MODE>(j0, b, a.bar, a.snap);
-            const float4 B2 = fetch_bar<MODE>(j2, b, a.bar, a.snap);
-            const float4 B4 = fetch_bar<MODE>(j4, b, a.bar, a.snap);
-            const float4 P = a.P4[p];
-            const float4 Q = a.Q4[p];
-            const float q5o = a.Q1[p];
-            float p0 = fadd(P.x, fmul(0.25f, fsub(fsub(B0.x, b.x), b.y)));
-            float p1 = fadd(P.y, fmul(0.25f, fsub(fsub(B2.x, b.x), b.z)));
-            float p2 = fadd(P.z, fmul(0.25f, fsub(fsub(B4.x, b.x), b.w)));
-            clip3(p0, p1, p2, a.alpha1);
-            const float e0 = fsub(B0.y, b.y);
-            const float e1 = fsub(B2.z, b.z);
-            const float e2 = fsub(B4.w, b.w);
-            const float e3 = fmul(0.5f, fsub(fadd(fsub(B2.y, b.y), B0.z), b.z));
-            const float e4 = fmul(0.5f, fsub(fadd(fsub(B4.y, b.y), B0.w), b.w));
-            const float e5 = fmul(0.5f, fsub(fadd(fsub(B4.z, b.z), B2.w), b.w));
-            float q[6] = {fadd(P.w, fmul(0.25f, e0)), fadd(Q.x, fmul(0.25f, e1)), fadd(Q.y, fmul(0.25f, e2)),
-                          fadd(Q.z, fmul(0.25f, e3)), fadd(Q.w, fmul(0.25f, e4)), fadd(q5o, fmul(0.25f, e5))};
-            clip6(q, a.alpha0);
-            a.P4[p] = make_float4(p0, p1, p2, q[0]);
-            a.Q4[p] = make_float4(q[1], q[2], q[3], q[4]);
-            a.Q1[p] = q[5];
-            if (RES) {
-                const double d0 = (double)p0 - P.x, d1 = (double)p1 - P.y, d2 = (double)p2 - P.z;
-                const double d3 = (double)q[0] - P.w, d4 = (double)q[1] - Q.x, d5 = (double)q[2] - Q.y;
-                const double d6 = (double)q[3] - Q.z, d7 = (double)q[4] - Q.w, d8 = (double)q[5] - q5o;
-                dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5 + d6 * d6 + d7 * d7 + d8 * d8;
-                nd = (double)p0 * p0 + (double)p1 * p1 + (double)p2 * p2;
+// One cube's dual ascent: p on |grad u - v| (radius alpha1) and q on |e(v)|
+// (radius alpha0), in the reference's operation order (tgv.cpp:158-189).
+// Returns the residual contributions through dd / nd when RES.
+template <int MODE, bool RES, bool CG>
+__device__ __forceinline__ void dual_cube(const IterArgs& a, int p, double& dd, double& nd) {
+    const float4 b = ld4<CG>(a.bar + p);
+    const int j0 = __ldg(a.nb + p), j2 = __ldg(a.nb + 2 * a.npos + p), j4 = __ldg(a.nb + 4 * a.npos + p);
+    const float4 B0 = fetch_bar<MODE, CG>(j0, b, a.bar, a.snap);
+    const float4 B2 = fetch_bar<MODE, CG>(j2, b, a.bar, a.snap);
+    const float4 B4 = fetch_bar<MODE, CG>(j4, b, a.bar, a.snap);
+    const float4 P = ld4<CG>(a.P4 + p);
+    const float4 Q = ld4<CG>(a.Q4 + p);
+    const float q5o = ld1<CG>(a.Q1 + p);
+    float p0 = fadd(P.x, fmul(0.25f, fsub(fsub(B0.x, b.x), b.y)));
+    float p1 = fadd(P.y, fmul(0.25f, fsub(fsub(B2.x, b.x), b.z)));
+    float p2 = fadd(P.z, fmul(0.25f, fsub(fsub(B4.x, b.x), b.w)));
+    clip3(p0, p1, p2, a.alpha1);
+    const float e0 = fsub(B0.y, b.y);
+    const float e1 = fsub(B2.z, b.z);
+    const float e2 = fsub(B4.w, b.w);
+    const float e3 = fmul(0.5f, fsub(fadd(fsub(B2.y, b.y), B0.z), b.z));
+    const float e4 = fmul(0.5f, fsub(fadd(fsub(B4.y, b.y), B0.w), b.w));
+    const float e5 = fmul(0.5f, fsub(fadd(fsub(B4.z, b.z), B2.w), b.w));
+    float q[6] = {fadd(P.w, fmul(0.25f, e0)), fadd(Q.x, fmul(0.25f, e1)), fadd(Q.y, fmul(0.25f, e2)),
+                  fadd(Q.z, fmul(0.25f, e3)), fadd(Q.w, fmul(0.25f, e4)), fadd(q5o, fmul(0.25f, e5))};
+    clip6(q, a.alpha0);
+    a.P4[p] = make_float4(p0, p1, p2, q[0]);
+    a.Q4[p] = make_float4(q[1], q[2], q[3], q[4]);
+    a.Q1[p] = q[5];
+    if (RES) {
+        const double d0 = (double)p0 - P.x, d1 = (double)p1 - P.y, d2 = (double)p2 - P.z;
+        const double d3 = (double)q[0] - P.w, d4 = (double)q[1] - Q.x, d5 = (double)q[2] - Q.y;
+        const double d6 = (double)q[3] - Q.z, d7 = (double)q[4] - Q.w, d8 = (double)q[5] - q5o;
+        dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5 + d6 * d6 + d7 * d7 + d8 * d8;
+        nd = (double)p0 * p0 + (double)p1 * p1 + (double)p2 * p2;
 #pragma unroll
-                for (int k = 0; k < 6; ++k) nd += (double)q[k] * q[k];
-            }
-        }
-        if (RES) wa.add(work ? slot : -1, dd, nd, a.acc, 1, lane);
+        for (int k = 0; k < 6; ++k) nd += (double)q[k] * q[k];
     }
-    if (RES) wa.flush(a.acc, 1, lane);
 }
 
-// K7: primal descent on u (prox of tot*|u - median|) and v, then extrapolation.
-template <int MODE, bool RES, bool STOP>
-__global__ void __launch_bounds__(ITER_BLOCK) k_primal(IterArgs a) {
+// One cube's primal descent: u by the prox of tot*|u - median|, v, then the
+// extrapolated bars (tgv.cpp:191-230).
+template <int MODE, bool RES, bool CG>
+__device__ __forceinline__ void primal_cube(const IterArgs& a, int p, double& dd, double& nd) {
+    const float4 U = ld4<CG>(a.uv + p);
+    const float4 P = ld4<CG>(a.P4 + p);
+    const float4 Q = ld4<CG>(a.Q4 + p);
+    const float q5 = ld1<CG>(a.Q1 + p);
+    const float2 D = __ldg(a.dat + p);
+    const int j1 = __ldg(a.nb + a.npos + p), j3 = __ldg(a.nb + 3 * a.npos + p), j5 = __ldg(a.nb + 5 * a.npos + p);
+    float gp10 = 0.f, gq10 = 0.f, gq13 = 0.f, gq14 = 0.f;
+    float gp31 = 0.f, gq31 = 0.f, gq33 = 0.f, gq35 = 0.f;
+    float gp52 = 0.f, gq52 = 0.f, gq54 = 0.f, gq55 = 0.f;
+    if (j1 >= 0 && !(MODE == M_STREAM && (j1 & BORDER))) {
+        const int j = j1 & POS_MASK;
+        const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
+        gp10 = a4.x; gq10 = a4.w; gq13 = b4.z; gq14 = b4.w;
+    }
+    if (j3 >= 0 && !(MODE == M_STREAM && (j3 & BORDER))) {
+        const int j = j3 & POS_MASK;
+        const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
+        gp31 = a4.y; gq31 = b4.x; gq33 = b4.z; gq35 = ld1<CG>(a.Q1 + j);
+    }
+    if (j5 >= 0 && !(MODE == M_STREAM && (j5 & BORDER))) {
+        const int j = j5 & POS_MASK;
+        const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
+        gp52 = a4.z; gq52 = b4.y; gq54 = b4.w; gq55 = ld1<CG>(a.Q1 + j);
+    }
+    const float p0 = P.x, p1 = P.y, p2 = P.z;
+    const float q0 = P.w, q1 = Q.x, q2 = Q.y, q3 = Q.z, q4 = Q.w;
+    const float div_p = fadd(fadd(fsub(p0, gp10), fsub(p1, gp31)), fsub(p2, gp52));
+    const float z = fadd(U.x, fmul(0.25f, div_p));
+    float un;
+    if (D.y < 0.0f) {
+        un = z;
+    } else {
+        const float diff = fsub(z, D.x);
+        if (diff > D.y) un = fsub(z, D.y);
+        else if (diff < -D.y) un = fadd(z, D.y);
+        else un = D.x;
+    }
+    const float dqx = fadd(fadd(fsub(q0, gq10), fsub(q3, gq33)), fsub(q4, gq54));
+    const float dqy = fadd(fadd(fsub(q3, gq13), fsub(q1, gq31)), fsub(q5, gq55));
+    const float dqz = fadd(fadd(fsub(q4, gq14), fsub(q5, gq35)), fsub(q2, gq52));
+    const float vxn = fadd(U.y, fmul(0.25f, fadd(p0, dqx)));
+    const float vyn = fadd(U.z, fmul(0.25f, fadd(p1, dqy)));
+    const float vzn = fadd(U.w, fmul(0.25f, fadd(p2, dqz)));
+    a.bar[p] = make_float4(fsub(fmul(2.0f, un), U.x), fsub(fmul(2.0f, vxn), U.y), fsub(fmul(2.0f, vyn), U.z),
+                           fsub(fmul(2.0f, vzn), U.w));
+    a.uv[p] = make_float4(un, vxn, vyn, vzn);
+    if (RES) {
+        const double d0 = (double)un - U.x, d1 = (double)vxn - U.y, d2 = (double)vyn - U.z, d3 = (double)vzn - U.w;
+        dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
+        nd = (double)un * un + (double)vxn * vxn + (double)vyn * vyn + (double)vzn * vzn;
+    }
+}
+
+// A block's share of one sweep over positions [beg, end): warps take 32-cube
+// groups in order (or in reverse order with REV, so that a sweep starts where
+// the previous one ended and finds its last writes still in L2).
+template <int MODE, bool RES, bool STOP, bool CG, bool DUAL, bool REV>
+__device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpAcc& wa) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int ngroups = (end - beg + 31) >> 5;
+    for (int gi = warp; gi < ngroups; gi += nw) {
+        const int g = REV ? (ngroups - 1 - gi) : gi;
+        const int p = beg + g * 32 + lane;
+        int slot = -1;
+        if (p < end) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
+        bool work = p < end;
+        if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
+        double dd = 0.0, nd = 0.0;
+        if (work) {
+            if (DUAL) dual_cube<MODE, RES, CG>(a, p, dd, nd);
+            else primal_cube<MODE, RES, CG>(a, p, dd, nd);
+        }
+        if (RES) wa.add(work ? slot : -1, dd, nd, a.acc, DUAL ? 1 : 0, lane);
+    }
+}
+
+// K6 / K7 as one launch per sweep.  The primal sweep runs in reverse block
+// order so it starts on the cubes whose p/q the dual sweep wrote last.
+// MINB = 8 caps registers at 32 so that 64 warps fit per SM (more loads in
+// flight); MINB = 6 (the default) allows about 42.
+template <int MODE, bool RES, bool STOP, int MINB>
+__global__ void __launch_bounds__(ITER_BLOCK, MINB) k_dual(IterArgs a) {
     if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int beg = a.o + blockIdx.x * a.chunk;
     const int end = min(a.o + a.n, beg + a.chunk);
     WarpAcc wa;
-    for (int g = beg + warp * 32; g < end; g += ITER_BLOCK) {
-        const int p = g + lane;
-        int slot = -1;
-        if (p < end) slot = (MODE == M_STREAM) ? a.lid[p] : a.slot0;
-        bool work = p < end;
-        if (STOP && work && MODE == M_STREAM) work = !a.done[slot];
-        double dd = 0.0, nd = 0.0;
-        if (work) {
-            const float4 U = a.uv[p];
-            const float4 P = a.P4[p];
-            const float4 Q = a.Q4[p];
-            const float q5 = a.Q1[p];
-            const float2 D = a.dat[p];
-            const int j1 = a.nb[a.npos + p], j3 = a.nb[3 * a.npos + p], j5 = a.nb[5 * a.npos + p];
-            float gp10 = 0.f, gq10 = 0.f, gq13 = 0.f, gq14 = 0.f;
-            float gp31 = 0.f, gq31 = 0.f, gq33 = 0.f, gq35 = 0.f;
-            float gp52 = 0.f, gq52 = 0.f, gq54 = 0.f, gq55 = 0.f;
-            if (j1 >= 0 && !(MODE == M_STREAM && (j1 & BORDER))) {
-                const int j = j1 & POS_MASK;
-                const float4 a4 = a.P4[j], b4 = a.Q4[j];
-                gp10 = a4.x; gq10 = a4.w; gq13 = b4.z; gq14 = b4.w;
-            }
-            if (j3 >= 0 && !(MODE == M_STREAM && (j3 & BORDER))) {
-                const int j = j3 & POS_MASK;
-                const float4 a4 = a.P4[j], b4 = a.Q4[j];
-                gp31 = a4.y; gq31 = b4.x; gq33 = b4.z; gq35 = a.Q1[j];
-            }
-            if (j5 >= 0 && !(MODE == M_STREAM && (j5 & BORDER))) {
-                const int j = j5 & POS_MASK;
-                const float4 a4 = a.P4[j], b4 = a.Q4[j];
-                gp52 = a4.z; gq52 = b4.y; gq54 = b4.w; gq55 = a.Q1[j];
-            }
-            const float p0 = P.x, p1 = P.y, p2 = P.z;
-            const float q0 = P.w, q1 = Q.x, q2 = Q.y, q3 = Q.z, q4 = Q.w;
-            const float div_p = fadd(fadd(fsub(p0, gp10), fsub(p1, gp31)), fsub(p2, gp52));
-            const float z = fadd(U.x, fmul(0.25f, div_p));
-            float un;
-            if (D.y < 0.0f) {
-                un = z;
-            } else {
-                const float diff = fsub(z, D.x);
-                if (diff > D.y) un = fsub(z, D.y);
-                else if (diff < -D.y) un = fadd(z, D.y);
-                else un = D.x;
-            }
-            const float dqx = fadd(fadd(fsub(q0, gq10), fsub(q3, gq33)), fsub(q4, gq54));
-            const float dqy = fadd(fadd(fsub(q3, gq13), fsub(q1, gq31)), fsub(q5, gq55));
-            const float dqz = fadd(fadd(fsub(q4, gq14), fsub(q5, gq35)), fsub(q2, gq52));
-            const float vxn = fadd(U.y, fmul(0.25f, fadd(p0, dqx)));
-            const float vyn = fadd(U.z, fmul(0.25f, fadd(p1, dqy)));
-            const float vzn = fadd(U.w, fmul(0.25f, fadd(p2, dqz)));
-            a.bar[p] = make_float4(fsub(fmul(2.0f, un), U.x), fsub(fmul(2.0f, vxn), U.y),
-                                   fsub(fmul(2.0f, vyn), U.z), fsub(fmul(2.0f, vzn), U.w));
-            a.uv[p] = make_float4(un, vxn, vyn, vzn);
-            if (RES) {
-                const double d0 = (double)un - U.x, d1 = (double)vxn - U.y, d2 = (double)vyn - U.z,
-                             d3 = (double)vzn - U.w;
-                dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
-                nd = (double)un * un + (double)vxn * vxn + (double)vyn * vyn + (double)vzn * vzn;
+    sweep<MODE, RES, STOP, false, true, false>(a, beg, end, wa);
+    if (RES) wa.flush(a.acc, 1, threadIdx.x & 31);
+}
+
+template <int MODE, bool RES, bool STOP, int MINB>
+__global__ void __launch_bounds__(ITER_BLOCK, MINB) k_primal(IterArgs a) {
+    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
+    const int blk = gridDim.x - 1 - blockIdx.x;
+    const int beg = a.o + blk * a.chunk;
+    const int end = min(a.o + a.n, beg + a.chunk);
+    WarpAcc wa;
+    sweep<MODE, RES, STOP, false, false, true>(a, beg, end, wa);
+    if (RES) wa.flush(a.acc, 0, threadIdx.x & 31);
+}
+
+// Grid-wide barrier of a co-resident (cooperatively launched) grid, with a
+// bounded wait: thread 0 of each block arrives on a counter; the last one
+// bumps the generation; the others poll it at most ~2^25 times (>= 1 s), then
+// set *err and give up, so a broken grid ends instead of hanging.
+__device__ __forceinline__ bool grid_sync(unsigned* count, unsigned* gen, int* err) {
+    __syncthreads();
+    if (gridDim.x > 1 && threadIdx.x == 0) {
+        volatile unsigned* vg = gen;
+        const unsigned g = *vg;
+        __threadfence();
+        if (atomicAdd(count, 1u) == gridDim.x - 1) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (*vg == g) {
+                if (++spins > (1u << 25)) { atomicOr(err, 1); break; }
+                __nanosleep(32);
             }
         }
-        if (RES) wa.add(work ? slot : -1, dd, nd, a.acc, 0, lane);
+        __threadfence();
     }
-    if (RES) wa.flush(a.acc, 0, lane);
+    __syncthreads();
+    return *(volatile int*)err == 0;
+}
+
+// Stopping test for all slots, run by block 0 between barriers (k_check's logic).
+__device__ __forceinline__ void check_slots(const IterArgs& a, int it) {
+    for (int s = threadIdx.x; s < a.nslot; s += blockDim.x) {
+        if (a.done[s]) continue;
+        double* q = a.acc + s * 4;
+        const double num = sqrt(__ldcg(q + 0)) + sqrt(__ldcg(q + 1));
+        const double den = sqrt(__ldcg(q + 2)) + sqrt(__ldcg(q + 3));
+        const double rel = den > 0.0 ? num / den : 0.0;
+        a.resid[s] = rel;
+        if (rel <= (double)a.tol) { a.done[s] = 1; a.iters_run[s] = it + 1; }
+        q[0] = q[1] = q[2] = q[3] = 0.0;
+    }
+}
+
+// Every iteration of one level in ONE cooperative launch (levels small enough
+// that launch latency, not bandwidth, dominates).  Blocks own contiguous
+// chunks; two grid barriers per iteration order the dual and primal sweeps.
+template <int MODE, bool STOP>
+__global__ void __launch_bounds__(ITER_BLOCK) k_level_persistent(IterArgs a) {
+    const int beg = a.o + blockIdx.x * a.chunk;
+    const int end = min(a.o + a.n, beg + a.chunk);
+    for (int i = 0; i < a.iters; ++i) {
+        const int it = a.it0 + i;
+        if (STOP && MODE != M_STREAM && *(volatile int*)(a.done + a.slot0)) break;
+        const bool res = STOP && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
+        WarpAcc wd, wp;
+        if (res) sweep<MODE, true, STOP, true, true, false>(a, beg, end, wd);
+        else sweep<MODE, false, STOP, true, true, false>(a, beg, end, wd);
+        if (res) wd.flush(a.acc, 1, threadIdx.x & 31);
+        if (!grid_sync(a.bar_count, a.bar_gen, a.err)) return;
+        if (res) sweep<MODE, true, STOP, true, false, false>(a, beg, end, wp);
+        else sweep<MODE, false, STOP, true, false, false>(a, beg, end, wp);
+        if (res) {
+            wp.flush(a.acc, 0, threadIdx.x & 31);
+            if (!grid_sync(a.bar_count, a.bar_gen, a.err)) return;
+            if (blockIdx.x == 0) check_slots(a, it);
+        }
+        if (!grid_sync(a.bar_count, a.bar_gen, a.err)) return;
+    }
 }
 
 // Stopping test after a residual iteration: relative fixed-point residual
@@ -561,15 +663,168 @@ __global__ void k_unpermute(int n, const int* __restrict__ inv, const float4* __
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 template <int MODE>
-static void launch_iter(tgvg_ctx* ctx, const IterArgs& a, bool res, bool stop, bool dual) {
+static void launch_iter(tgvg_ctx* ctx, IterArgs a, bool res, bool stop, bool dual, bool lean) {
+    // One full wave: as many blocks as fit on the GPU at once (occupancy of the
+    // plain variant), each owning an equal contiguous chunk of the unit.
+    const int occ = ctx->iter_occ[MODE][lean ? 1 : 0][dual ? 0 : 1];
+    const int want = std::max(1, std::min((a.n + ITER_BLOCK - 1) / ITER_BLOCK, occ * ctx->sm_count));
+    a.chunk = ((a.n + want - 1) / want + 31) / 32 * 32;
     const unsigned grid = (unsigned)((a.n + a.chunk - 1) / a.chunk);
-#define TGVG_ITER(K)                                                                  \
-    if (res && stop) K<MODE, true, true><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);    \
-    else if (res) K<MODE, true, false><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);      \
-    else if (stop) K<MODE, false, true><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);     \
-    else K<MODE, false, false><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);
+#define TGVG_ITER(K)                                                                    \
+    if (res && stop) K<MODE, true, true, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
+    else if (res) K<MODE, true, false, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);     \
+    else if (stop) K<MODE, false, true, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);    \
+    else if (lean) K<MODE, false, false, 8><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
+    else K<MODE, false, false, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);
     if (dual) { TGVG_ITER(k_dual) } else { TGVG_ITER(k_primal) }
 #undef TGVG_ITER
+}
+
+// Blocks per SM of the plain (and register-capped) sweep kernels, per mode.
+template <int MODE>
+static int iter_occupancy(tgvg_ctx* ctx) {
+    int* o = &ctx->iter_occ[MODE][0][0];
+    if (o[0] > 0) return TGVG_OK;
+    int v[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v[0], k_dual<MODE, false, false, 6>, ITER_BLOCK, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v[1], k_primal<MODE, false, false, 6>, ITER_BLOCK, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v[2], k_dual<MODE, false, false, 8>, ITER_BLOCK, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v[3], k_primal<MODE, false, false, 8>, ITER_BLOCK, 0);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy query");
+    o[0] = std::max(1, v[0]); o[1] = std::max(1, v[1]); o[2] = std::max(1, v[2]); o[3] = std::max(1, v[3]);
+    return TGVG_OK;
+}
+
+// ---- launch schedules of one unit (a level, or one leaf's slice of it in OC) ----
+// cfg 0: two launches per iteration (K6, K7) over a grid of up to 8 blocks per SM.
+// cfg k in 1..6: one cooperative launch of k_level_persistent running all the
+//   unit's iterations, with about 256 << k cubes per block.
+// Every schedule applies the identical per-cube arithmetic, so the choice never
+// changes a result, only the time.
+// cfg 7 (CFG_LEAN): as cfg 0 with the sweep kernels capped at 32 registers.
+static constexpr int TUNE_SEG = 16;
+static constexpr int N_PERSIST_CFG = 6;
+static constexpr int CFG_LEAN = 7;
+
+static int persist_grid(int n, int cfg, int cmax) {
+    const int cpb = 256 << cfg;
+    return std::max(1, std::min((n + cpb - 1) / cpb, cmax));
+}
+
+template <int MODE>
+static int coop_capacity(tgvg_ctx* ctx, bool stop, int* out) {
+    int& cmax = ctx->coop_max[MODE][stop ? 1 : 0];
+    if (cmax <= 0) {
+        int per = 0;
+        cudaError_t e = stop ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_level_persistent<MODE, true>,
+                                                                            ITER_BLOCK, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_level_persistent<MODE, false>,
+                                                                            ITER_BLOCK, 0);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy query");
+        cmax = std::max(1, per) * ctx->sm_count;
+    }
+    *out = cmax;
+    return TGVG_OK;
+}
+
+template <int MODE>
+static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, bool stop, bool timed) {
+    if (count <= 0) return TGVG_OK;
+    if (cfg == 0 || cfg == CFG_LEAN) {
+        const bool lean = cfg == CFG_LEAN;
+        int rc = iter_occupancy<MODE>(ctx);
+        if (rc) return rc;
+        for (int it = it0; it < it0 + count; ++it) {
+            const bool res = stop && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
+            if (timed) cudaEventRecord(ctx->tev[3 * it], ctx->stream);
+            launch_iter<MODE>(ctx, a, res, stop, true, lean);
+            if (timed) cudaEventRecord(ctx->tev[3 * it + 1], ctx->stream);
+            launch_iter<MODE>(ctx, a, res, stop, false, lean);
+            if (timed) cudaEventRecord(ctx->tev[3 * it + 2], ctx->stream);
+            cudaError_t le = cudaGetLastError();
+            if (le != cudaSuccess) return ctx->cuda_fail(le, "iteration launch");
+            ctx->kernels += 2;
+            if (res) {
+                k_check<<<blocks_for(a.nslot, 128), 128, 0, ctx->stream>>>(a.nslot, a.acc, a.done, a.tol, it,
+                                                                          a.iters_run, a.resid);
+                TGVG_LAUNCHED(ctx);
+            }
+        }
+        return TGVG_OK;
+    }
+    int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
+    if (rc) return rc;
+    const int G = persist_grid(a.n, cfg, cmax);
+    a.chunk = ((a.n + G - 1) / G + 31) / 32 * 32;
+    const unsigned grid = (unsigned)((a.n + a.chunk - 1) / a.chunk);
+    a.it0 = it0;
+    a.iters = count;
+    TGVG_CK(ctx, cudaMemsetAsync(a.bar_count, 0, sizeof(unsigned), ctx->stream));
+    void* args[] = {&a};
+    cudaError_t e = stop ? cudaLaunchCooperativeKernel((const void*)k_level_persistent<MODE, true>, dim3(grid),
+                                                       dim3(ITER_BLOCK), args, 0, ctx->stream)
+                         : cudaLaunchCooperativeKernel((const void*)k_level_persistent<MODE, false>, dim3(grid),
+                                                       dim3(ITER_BLOCK), args, 0, ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cooperative launch");
+    ++ctx->kernels;
+    return TGVG_OK;
+}
+
+// Run `iters` iterations of one unit.  The schedule for the unit's size class
+// (floor(log2 n)) is taken from the context's table; the first time a class
+// is met in a fixed-count solve with enough iterations, its first segments
+// try each candidate schedule for TUNE_SEG iterations and keep the fastest
+// (online autotuning: the tried iterations count toward the solve).
+template <int MODE>
+static int run_unit_t(tgvg_ctx* ctx, IterArgs& a, int iters, bool stop, bool timed, int* used) {
+    const int cls = 31 - __builtin_clz((unsigned)std::max(1, a.n));
+    int& tuned = ctx->tune[MODE][cls];
+    int it = 0, cfg;
+    if (timed) {
+        cfg = 0;  // per-launch event timing needs the per-sweep launches
+    } else if (tuned >= 0) {
+        cfg = tuned;
+    } else {
+        int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
+        if (rc) return rc;
+        std::vector<int> cands = {0, CFG_LEAN};
+        int last_grid = -1;
+        if (a.n <= (1 << 22))
+            for (int k = 1; k <= N_PERSIST_CFG; ++k) {
+                const int g = persist_grid(a.n, k, cmax);
+                if (g != last_grid) cands.push_back(k);
+                last_grid = g;
+            }
+        if (!stop && (int)cands.size() * TUNE_SEG * 2 <= iters) {
+            float best_ms = 1e30f;
+            int best = 0;
+            for (int c : cands) {
+                TGVG_CK(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+                if ((rc = run_segment<MODE>(ctx, a, c, it, TUNE_SEG, stop, false))) return rc;
+                TGVG_CK(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+                TGVG_CK(ctx, cudaEventSynchronize(ctx->ev[3]));
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+                if (ms < best_ms) { best_ms = ms; best = c; }
+                it += TUNE_SEG;
+            }
+            tuned = best;
+            cfg = best;
+        } else {
+            cfg = a.n <= 65536 ? 3 : 0;  // untuned default: one cooperative launch for small units
+        }
+    }
+    *used = cfg;
+    return run_segment<MODE>(ctx, a, cfg, it, iters - it, stop, timed);
+}
+
+static int run_unit(tgvg_ctx* ctx, int mode, IterArgs& a, int iters, bool stop, bool timed, int* used) {
+    if (mode == M_INMEM) return run_unit_t<M_INMEM>(ctx, a, iters, stop, timed, used);
+    if (mode == M_OC) return run_unit_t<M_OC>(ctx, a, iters, stop, timed, used);
+    return run_unit_t<M_STREAM>(ctx, a, iters, stop, timed, used);
 }
 
 int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists, int64_t n64,
@@ -667,7 +922,9 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         hostleaf[3 * std::max(1, nsl) + std::max(1, L) + l] = ll[l];
     }
     TGVG_CK(ctx, cudaMemcpyAsync(lv, hostleaf.data(), 4 * hostleaf.size(), cudaMemcpyHostToDevice, ctx->stream));
-    const int init_flags[4] = {0, 0, 21, 0};
+    // [0] unsorted [1] bad depth [2] min depth [3] max depth [4] barrier count [5] barrier
+    // generation [6] bounded-wait timeout [7] unused
+    const int init_flags[8] = {0, 0, 21, 0, 0, 0, 0, 0};
     TGVG_CK(ctx, cudaMemcpyAsync(flags, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice, ctx->stream));
 
     // ---- K3: keys, leaves, level-major order, hash, neighbours
@@ -732,7 +989,6 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     // ---- levels
     const bool stop = prm->tol > 0.0f && prm->check_every > 0;
     const int iters = std::max(0, prm->iters);
-    const int per_sm = 8;
     st.min_depth = min_d;
     st.max_depth = max_d;
     std::vector<int> h_iters(nslot);
@@ -755,8 +1011,12 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     for (int Ld = min_d; Ld <= max_d; ++Ld) {
         const int o = h_bstart[Ld], cnt = h_bstart[Ld + 1] - h_bstart[Ld];
         if (cnt <= 0) continue;
+        const int slot = st.n_levels;
+        if (slot < TGVG_MAX_LEVELS) cudaEventRecord(ctx->lev_ev[2 * slot], ctx->stream);
+        int used_cfg = -1;
         if (Ld > min_d) {
-            k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, par, uv, bar, P4, Q4, Q1);
+            k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, par, prm->keep_init_u ? 1 : 0, uv,
+                                                                          bar, P4, Q4, Q1);
             TGVG_LAUNCHED(ctx);
         }
         if (mode == M_STREAM) {
@@ -789,38 +1049,25 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         nvtxRangePushA(Ld == big_level ? "tgv_largest_level" : "tgv_level");
         for (const Unit& u : us) {
             IterArgs a;
+            std::memset(&a, 0, sizeof(a));
             a.o = u.o; a.n = u.n; a.npos = n;
-            const int want = std::max(1, std::min((u.n + ITER_BLOCK - 1) / ITER_BLOCK, ctx->sm_count * per_sm));
-            a.chunk = ((u.n + want - 1) / want + 31) / 32 * 32;
             a.nb = nb; a.uv = uv; a.bar = bar; a.P4 = P4; a.Q4 = Q4; a.Q1 = Q1; a.dat = dat; a.snap = snap;
             a.lid = lid; a.acc = acc; a.done = done; a.slot0 = u.slot;
             a.alpha0 = prm->alpha0; a.alpha1 = prm->alpha1;
-            const bool timed = Ld == t_level;
-            for (int it = 0; it < iters; ++it) {
-                const bool res = stop && ((it + 1) % prm->check_every == 0 || it + 1 == iters);
-                if (timed) cudaEventRecord(ctx->tev[3 * it], ctx->stream);
-                if (mode == M_INMEM) launch_iter<M_INMEM>(ctx, a, res, stop, true);
-                else if (mode == M_OC) launch_iter<M_OC>(ctx, a, res, stop, true);
-                else launch_iter<M_STREAM>(ctx, a, res, stop, true);
-                if (timed) cudaEventRecord(ctx->tev[3 * it + 1], ctx->stream);
-                if (mode == M_INMEM) launch_iter<M_INMEM>(ctx, a, res, stop, false);
-                else if (mode == M_OC) launch_iter<M_OC>(ctx, a, res, stop, false);
-                else launch_iter<M_STREAM>(ctx, a, res, stop, false);
-                if (timed) cudaEventRecord(ctx->tev[3 * it + 2], ctx->stream);
-                cudaError_t le = cudaGetLastError();
-                if (le != cudaSuccess) return ctx->cuda_fail(le, "iteration launch");
-                ctx->kernels += 2;
-                if (res) {
-                    k_check<<<blocks_for(nslot, 128), 128, 0, ctx->stream>>>(nslot, acc, done, prm->tol, it,
-                                                                             iters_run, resid);
-                    TGVG_LAUNCHED(ctx);
-                }
-            }
+            a.check_every = std::max(1, prm->check_every); a.nslot = nslot; a.tol = prm->tol; a.iters_total = iters;
+            a.bar_count = reinterpret_cast<unsigned*>(flags + 4);
+            a.bar_gen = reinterpret_cast<unsigned*>(flags + 5);
+            a.err = flags + 6;
+            a.iters_run = iters_run; a.resid = resid;
+            const int rc = run_unit(ctx, mode, a, iters, stop, Ld == t_level, &used_cfg);
+            if (rc) return rc;
         }
         nvtxRangePop();
+        if (slot < TGVG_MAX_LEVELS) cudaEventRecord(ctx->lev_ev[2 * slot + 1], ctx->stream);
         // level stats
         if (st.n_levels < TGVG_MAX_LEVELS) {
             const int k = st.n_levels++;
+            st.schedule[k] = used_cfg;
             st.depth[k] = Ld;
             st.active[k] = cnt;
             if (stop) {
@@ -855,7 +1102,10 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     TGVG_CK(ctx, cudaEventRecord(e2, ctx->stream));
     k_unpermute<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, inv, uv, P4, Q4, Q1, reinterpret_cast<float*>(d_out));
     TGVG_LAUNCHED(ctx);
+    int h_err = 0;
+    TGVG_CK(ctx, cudaMemcpyAsync(&h_err, flags + 6, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h_err) return ctx->fail(TGVG_ERR_TIMEOUT, "a grid barrier of the persistent iteration kernel timed out");
     float ms_setup = 0.f, ms_iter = 0.f;
     cudaEventElapsedTime(&ms_setup, e0, e1);
     cudaEventElapsedTime(&ms_iter, e1, e2);
@@ -863,6 +1113,11 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     st.iterate_ms = ms_iter;
     st.total_ms = ms_setup + ms_iter;
     st.kernel_launches = (int32_t)(ctx->kernels - k0);
+    for (int k = 0; k < st.n_levels; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->lev_ev[2 * k], ctx->lev_ev[2 * k + 1]);
+        st.level_ms[k] = ms;
+    }
     if (t_level >= 0) {
         double dsum = 0.0, psum = 0.0;
         for (int it = 0; it < iters; ++it) {
