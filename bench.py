@@ -5,8 +5,10 @@ One step = one full coarse-to-fine solve (setup + every level, fixed iteration
 count per level) over one synthetic workload with inputs resident in HBM.  The
 default workload, three64, has the shape of the "plain method at scale"
 configuration: a sphere, a box and a torus seen by 64 cameras at 1920x1080,
-cubes to depth 11 (about 20M), 10-bin histograms from this package's own
-kernels, alpha1 = 1, alpha0 = 2, 1000 iterations per level.
+cubes to depth 11 (6.2M with seed 0), 10-bin histograms from this package's
+own kernels, alpha1 = 1, alpha0 = 2, 1000 iterations per level.  The first
+warm-up step lets the online autotuner pick each level's schedule; later steps
+capture the level loop into a CUDA graph and relaunch it.
 
 Also reported in the same JSON line:
   e2e           the same metric through the public host-buffer C ABI call
@@ -15,6 +17,10 @@ Also reported in the same JSON line:
                 on the library's stream, against MEASURED_PEAKS.json
   cpu_baseline  the CPU oracle port on a bounded sample of the same workload
   histograms    the Stage-5 pass (pyramids + binning) on the same workload
+  warm_start    time to relative residual 1e-4 on held-out small scenes from
+                the zero start, from the trained warm-start network
+                (tgvreconclaude_gb300/data/warmstart_nb10.npz) and from the
+                reference's initialisation
 
 `--impl reference` times the CPU implementation of the path (the oracle port of
 the reference's tgv.cpp, all host threads) on a bounded sample of the same
@@ -250,6 +256,36 @@ def measure_e2e(args, w, ctx, prm, mode, leaves, out_t, stream):
             "d2h_bytes_per_step": int(52 * n), "steps": steps, "wall_s": t_wall, "matches_device_run": same}
 
 
+def warm_start_eval(args):
+    """Time to relative residual 1e-4 (at most 6000 iterations per level) on
+    held-out small scenes: zero start, trained network, reference initialisation."""
+    from tgvreconclaude_gb300 import api, warmstart as WS
+    path = os.path.join(HERE, "tgvreconclaude_gb300", "data", "warmstart_nb10.npz")
+    if not os.path.exists(path):
+        return {"unavailable": "no trained weights at tgvreconclaude_gb300/data/warmstart_nb10.npz"}
+    mlp = WS.WarmStartMLP.load(path)
+    recs = []
+    for seed in range(1000, 1000 + args.warm_seeds):
+        kind = "torus" if seed % 2 == 0 else "three"
+        cubes, hists = WS.small_scene(seed, kind)
+        zero, warm, _ = WS.compare(mlp, cubes, hists, tol=1e-4)
+        prm = api.TGVParams(alpha0=WS.SOLVE["alpha0"], alpha1=WS.SOLVE["alpha1"], iters=6000, tol=1e-4,
+                            check_every=10)
+        _, st = api.tgv_solve(cubes, hists, None, "inmem", prm)
+        recs.append(dict(seed=seed, kind=kind, cubes=int(len(cubes)), zero_ms=zero.device_ms,
+                         warm_ms=warm.device_ms + warm.predict_ms, ref_ms=st["total_ms"],
+                         zero_leaf_iters=zero.leaf_iters, warm_leaf_iters=warm.leaf_iters,
+                         ref_leaf_iters=st["leaf_iters"],
+                         capped_levels=[sum(i >= 6000 for i in r) for r in (zero.iters, warm.iters, st["iters_run"])]))
+    med = lambda k: float(np.median([r[k] for r in recs]))
+    return {"tol": 1e-4, "max_iters_per_level": 6000, "scenes": len(recs),
+            "scene": "16 cameras at 320x240, torus (depth 7) / three objects (depth 8), held-out seeds 1000+",
+            "median_zero_ms": med("zero_ms"), "median_warm_ms": med("warm_ms"), "median_ref_ms": med("ref_ms"),
+            "time_ratio_zero_over_warm": float(np.median([r["zero_ms"] / r["warm_ms"] for r in recs])),
+            "leaf_iters_ratio_zero_over_warm": med("zero_leaf_iters") / med("warm_leaf_iters"),
+            "records": recs}
+
+
 def run_ours(args):
     import torch
     ws, rank, local, pg = dist_setup()
@@ -277,12 +313,16 @@ def run_ours(args):
     leaves = w.leaves if mode == "stream" else None
     stream = torch.cuda.ExternalStream(ctx.stream)
 
-    for _ in range(args.warmup):
+    # warm-up: the first step autotunes every level's schedule (direct launches);
+    # with per-launch timing on, the next one captures the level loop into a
+    # CUDA graph that the timed steps relaunch
+    for k in range(args.warmup):
+        ctx.lib.tgvg_set_timing(ctx.h, int(k > 0))
         api.tgv_solve_device(cubes_t, hists_t, out_t, leaves, mode, prm)
+    ctx.lib.tgvg_set_timing(ctx.h, 1)
     torch.cuda.synchronize()
     if pg:
         pg.barrier()
-    ctx.lib.tgvg_set_timing(ctx.h, 1)
     clocks = Clocks(local)
     clocks.start()
     k0 = ctx.kernel_count()
@@ -346,6 +386,8 @@ def run_ours(args):
                   "sample": f"{len(cubes_s)} contiguous Morton-ordered cubes of {args.workload}, {args.cpu_iters} iterations per "
                             f"level, in-memory semantics, single thread"}
 
+        ws_eval = {} if args.skip_warm else warm_start_eval(args)
+
         depth_hist = np.bincount(w.cubes["depth"], minlength=22)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -358,7 +400,8 @@ def run_ours(args):
                        "chunks": len(w.leaves), "levels": {int(k): int(v) for k, v in enumerate(depth_hist) if v},
                        "l2": "inputs larger than L2 (about 100 B of state per cube)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "histograms": hs, "clocks": clk,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "histograms": hs, "warm_start": ws_eval,
+            "clocks": clk, "graph": last_st["graph"],
             "gpu_launches": int(launches), "leaf_iters_per_step": int(li_all / args.steps),
             "levels_detail": [{"depth": d, "active": int(a), "ms": round(m, 3), "schedule": s}
                               for d, a, m, s in zip(last_st["depth"], last_st["active"], last_st["level_ms"],
@@ -388,6 +431,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-hist", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-warm", action="store_true")
+    ap.add_argument("--warm-seeds", type=int, default=6)
     ap.add_argument("--max-cubes", type=int, default=0, help="truncate the workload (profiling runs)")
     ap.add_argument("--cache", default="", help="load the workload from / save it to this .npz (profiling runs)")
     args = ap.parse_args()

@@ -109,11 +109,15 @@ typedef struct tgvg_stats {
     double residual[TGVG_MAX_LEVELS];    /* last relative residual (max over leaves)*/
     int64_t leaf_iters;                  /* sum over levels of active x iterations  */
     int32_t kernel_launches;             /* kernels this call enqueued              */
-    int32_t reserved;
+    int32_t graph;                       /* level loop: 0 direct launches, 1 captured
+                                            into a new CUDA graph and launched, 2 a
+                                            cached graph of the same problem relaunched */
     double setup_ms, iterate_ms, total_ms; /* device time of the phases             */
     /* Per-launch timing of the iteration kernels on the level with the most
-     * active cubes (filled when tgvg_set_timing(ctx, 1) is on): summed CUDA
-     * event durations on the context stream and the launch count per kernel. */
+     * active cubes (filled when tgvg_set_timing(ctx, 1) is on): CUDA event
+     * durations on the context stream, summed over the launches of every 10th
+     * iteration, and the number of launches timed per kernel.  That level then
+     * runs with per-sweep launches (schedule 0, or 7 when tuned to it). */
     int32_t kt_depth;
     int32_t kt_launches;
     int64_t kt_active;
@@ -148,9 +152,19 @@ int tgvg_set_timing(tgvg_ctx* ctx, int on);
 /* Iteration schedule of a level whose active count n has floor(log2 n) == cls
  * (cls = -1: every class), for one mode: 0 = two launches per iteration, 1..6 =
  * one cooperative launch per level with about 256 << k cubes per block, 7 = as 0
- * with the sweep kernels capped at 32 registers, -1 = let the online autotuner
- * choose (default).  Results do not depend on it. */
+ * with the sweep kernels capped at 32 registers, 8 / 9 = as 0 / 7 with an L2
+ * prefetch of each warp's next group, -1 = let the online autotuner choose
+ * (default).  Results do not depend on it. */
 int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
+/* CUDA graphs for the level loop (1 = on, the default; 0 = off).  When every
+ * level's schedule is already fixed (chosen by the autotuner in an earlier
+ * call, set with tgvg_set_schedule, or the default of a tolerance-stopped
+ * solve) and per-launch timing is off, the whole level loop -- parent init,
+ * snapshots, the iteration launches and the stopping tests of every level --
+ * is captured into one CUDA graph, kept in the context and relaunched by the
+ * next solve of a problem with the same level sizes, leaves, parameters and
+ * buffers.  Results do not depend on it. */
+int tgvg_set_graphs(tgvg_ctx* ctx, int on);
 
 /* ---- Stage 5: depth maps -> histograms ------------------------------------ */
 
@@ -244,6 +258,41 @@ int tgvg_tgv_minimize_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_
 int tgvg_tgv_minimize_streaming(tgvg_ctx* ctx, const char* cube_path, const char* hist_path,
                                 const char* treetop_path, const char* out_state_path,
                                 const tgvg_params* params, tgvg_stats* stats);
+
+/* ---- learned warm start (no counterpart in the reference) -------------------
+ * A per-cube MLP F -> 64 -> 64 -> 1 (F = nbins + 5: histogram / total,
+ * depth / 21, the cube centre's position in its chunk's node, the median
+ * indicator), ReLU, BF16 weights and activations with FP32 accumulation on the
+ * tensor cores.  It is trained on (features, converged u - median indicator)
+ * pairs from the plain solver; the warm-start u is median indicator + network
+ * (tgvg_mlp_warm_start).  Solve with params.init = TGVG_INIT_GIVEN and
+ * keep_init_u = 1.  Features are 16 bf16 values per cube (uint16 bit
+ * patterns, zero padded). */
+typedef struct tgvg_mlp tgvg_mlp;
+int tgvg_mlp_create(tgvg_ctx* ctx, int32_t nbins, uint64_t seed, tgvg_mlp** out);
+int tgvg_mlp_destroy(tgvg_mlp* m);
+int32_t tgvg_mlp_num_params(void);
+/* Copy the fp32 parameters out (get) and/or in (set); either may be null. */
+int tgvg_mlp_params(tgvg_ctx* ctx, tgvg_mlp* m, float* get, const float* set);
+/* Features of n cubes (host arrays in and out). */
+int tgvg_mlp_features(tgvg_ctx* ctx, const tgvg_cube* cubes, const uint32_t* hists, int64_t n,
+                      int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, uint16_t* X);
+/* Prediction for n feature rows (host arrays). */
+int tgvg_mlp_predict(tgvg_ctx* ctx, tgvg_mlp* m, const uint16_t* X, int64_t n, float* y);
+/* Warm-start u of n cubes: features, forward pass and the median indicator
+ * (FP32, reference order) added, all on the device.  Host arrays in and out;
+ * the _dev form takes device cubes / histograms / u and host leaves, and
+ * leaves u on the context stream for tgvg_tgv_minimize_dev. */
+int tgvg_mlp_warm_start(tgvg_ctx* ctx, tgvg_mlp* m, const tgvg_cube* cubes, const uint32_t* hists, int64_t n,
+                        int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, float* u);
+int tgvg_mlp_warm_start_dev(tgvg_ctx* ctx, tgvg_mlp* m, const tgvg_cube* d_cubes, const uint32_t* d_hists,
+                            int64_t n, int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, float* d_u);
+/* Gradient of the mean squared error over all n rows (for checks; host arrays). */
+int tgvg_mlp_grad(tgvg_ctx* ctx, tgvg_mlp* m, const uint16_t* X, const float* t, int64_t n, float* grad,
+                  float* loss);
+/* Adam training over shuffled mini-batches; last_loss = mean loss of the last epoch. */
+int tgvg_mlp_train(tgvg_ctx* ctx, tgvg_mlp* m, const uint16_t* X, const float* t, int64_t n, int32_t epochs,
+                   int32_t batch, float lr, uint64_t seed, float* last_loss);
 
 /* ---- state / histogram files (reference tgv.cpp:24-46, histogram.cpp:175-218) */
 int tgvg_save_tgv(const char* path, const tgvg_state* state, int64_t n);

@@ -170,18 +170,58 @@ def test_tgv_random_vs_oracle(oracle_lib, seed):
 
 
 def test_tgv_autotuned_schedules_are_exact(oracle_lib):
-    """300 iterations: the first solve tunes each level's schedule online
-    (per-sweep launches vs one cooperative launch per level, several grid
-    sizes), the second reuses the tuned table; both stay bit-identical."""
+    """400 iterations: the first solve tunes each level's schedule online
+    (per-sweep launches with and without register cap and L2 prefetch vs one
+    cooperative launch per level, several grid sizes), the second reuses the
+    tuned table; both stay bit-identical."""
     rng = np.random.default_rng(77)
     cubes = S.random_octree(rng, dmin=1, dmax=7, target=60000, shape="sphere")
     hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.05)
     leaves = S.split_leaves(len(cubes), 5, rng, cubes, aligned=True)
     for mode in ("inmem", "stream"):
-        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, alpha0=2.0, alpha1=1.0, iters=300, nthreads=8)
+        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, alpha0=2.0, alpha1=1.0, iters=400, nthreads=8)
         for _ in range(2):
-            out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=300))
+            out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=400))
             assert_state_equal(out, ref, f"autotuned {mode}")
+
+
+@pytest.mark.parametrize("mode", ["inmem", "oc", "stream"])
+def test_tgv_graph_capture_and_replay(oracle_lib, mode):
+    """With the schedule fixed, the whole level loop is captured into one CUDA
+    graph (graph = 1) and relaunched for the same problem (graph = 2).  A
+    tolerance-stopped solve: graphs off, captured and replayed all give the
+    oracle's state and per-level iteration counts bit for bit.  A fixed-count
+    solve after resetting the schedule table: the first call autotunes with
+    direct launches (graph = 0), the next two capture and replay."""
+    ctx = api.context()
+    rng = np.random.default_rng(31)
+    cubes = S.random_octree(rng, dmin=1, dmax=6, target=20000, shape="sphere")
+    hists = S.random_histograms(rng, len(cubes), nbins=10, empty_frac=0.0)
+    leaves = S.split_leaves(len(cubes), 7, rng, cubes, aligned=True)
+    ref, rst = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 400, tol=1e-4, check_every=10,
+                                    nthreads=8)
+    prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=400, tol=1e-4, check_every=10)
+    try:
+        runs = []
+        for graphs in (False, True, True):
+            ctx.set_graphs(graphs)
+            runs.append(api.tgv_solve(cubes, hists, leaves, mode, prm))
+        assert [st["graph"] for _, st in runs] == [0, 1, 2]
+        for out, st in runs:
+            assert_state_equal(out, ref, f"graph {st['graph']} {mode}")
+            assert st["iters_run"] == [r["iters_run"] for r in rst]
+        assert runs[1][1]["kernel_launches"] == runs[2][1]["kernel_launches"] > 0
+
+        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 400, nthreads=8)
+        ctx.set_schedule(mode, -1, -1)
+        prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=400)
+        runs = [api.tgv_solve(cubes, hists, leaves, mode, prm) for _ in range(3)]
+        assert [st["graph"] for _, st in runs] == [0, 1, 2]
+        for out, st in runs:
+            assert_state_equal(out, ref, f"tuned graph {st['graph']} {mode}")
+        assert runs[1][1]["schedule"] == runs[2][1]["schedule"]
+    finally:
+        ctx.set_graphs(True)
 
 
 def test_tgv_unsorted_inmem_and_leaf_gaps(oracle_lib):
@@ -203,7 +243,7 @@ def test_tgv_unsorted_inmem_and_leaf_gaps(oracle_lib):
 
 
 def test_tgv_stopping_rule(oracle_lib):
-    """Per-level (per-leaf in streaming) stop at relative residual <= tol.  A
+    """Per-level (per-leaf in OC and streaming) stop at relative residual <= tol.  A
     level that stops early has residual <= tol; the iteration counts and the
     final state agree with the oracle.  (Cubes without votes make the
     reference's iteration drift, so some levels may run to the cap.)"""
@@ -212,7 +252,7 @@ def test_tgv_stopping_rule(oracle_lib):
     h = S.random_histograms(rng, len(cubes), empty_frac=0.0)
     h[h.sum(1) == 0, 3] = 1
     leaves = S.split_leaves(len(cubes), 3, rng, cubes, aligned=True)
-    for mode in ("inmem", "stream"):
+    for mode in ("inmem", "oc", "stream"):
         ref, rst = oracle_lib.tgv_solve(cubes, h, leaves, mode, 1.0, 2.0, 1500, tol=1e-4, check_every=10)
         out, st = api.tgv_solve(cubes, h, leaves, mode, api.TGVParams(1.0, 2.0, 1500, tol=1e-4, check_every=10))
         assert [r["iters_run"] for r in rst] == st["iters_run"], mode

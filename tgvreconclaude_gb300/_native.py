@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libtgvg.so")
-SOURCES = ["capi.cu", "hist.cu", "tgv.cu"]
+SOURCES = ["capi.cu", "hist.cu", "tgv.cu", "mlp.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
@@ -92,7 +92,7 @@ class Stats(C.Structure):
     _fields_ = [("n_levels", C.c_int32), ("min_depth", C.c_int32), ("max_depth", C.c_int32),
                 ("depth", C.c_int32 * MAX_LEVELS), ("active", C.c_int64 * MAX_LEVELS),
                 ("iters_run", C.c_int32 * MAX_LEVELS), ("residual", C.c_double * MAX_LEVELS),
-                ("leaf_iters", C.c_int64), ("kernel_launches", C.c_int32), ("reserved", C.c_int32),
+                ("leaf_iters", C.c_int64), ("kernel_launches", C.c_int32), ("graph", C.c_int32),
                 ("setup_ms", C.c_double), ("iterate_ms", C.c_double), ("total_ms", C.c_double),
                 ("kt_depth", C.c_int32), ("kt_launches", C.c_int32), ("kt_active", C.c_int64),
                 ("kt_dual_ms", C.c_double), ("kt_primal_ms", C.c_double),
@@ -103,7 +103,7 @@ class Stats(C.Structure):
         return dict(n_levels=k, min_depth=self.min_depth, max_depth=self.max_depth,
                     depth=list(self.depth[:k]), active=list(self.active[:k]),
                     iters_run=list(self.iters_run[:k]), residual=list(self.residual[:k]),
-                    leaf_iters=self.leaf_iters, kernel_launches=self.kernel_launches,
+                    leaf_iters=self.leaf_iters, kernel_launches=self.kernel_launches, graph=self.graph,
                     setup_ms=self.setup_ms, iterate_ms=self.iterate_ms, total_ms=self.total_ms,
                     kt_depth=self.kt_depth, kt_launches=self.kt_launches, kt_active=self.kt_active,
                     kt_dual_ms=self.kt_dual_ms, kt_primal_ms=self.kt_primal_ms,
@@ -122,6 +122,7 @@ _SIGS = {
     "tgvg_level_thresholds": ([P], None),
     "tgvg_set_timing": ([P, C.c_int], C.c_int),
     "tgvg_set_schedule": ([P, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+    "tgvg_set_graphs": ([P, C.c_int], C.c_int),
     "tgvg_pyramid_dims": ([C.c_int32, C.c_int32, P], C.c_int),
     "tgvg_build_pyramids": ([P, P, C.c_int32, P, P], C.c_int),
     "tgvg_compute_histograms": ([P, P, C.c_int64, P, C.c_int32, P, P, C.c_float, C.c_int32, P], C.c_int),
@@ -134,6 +135,16 @@ _SIGS = {
     "tgvg_tgv_minimize": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P], C.c_int),
     "tgvg_tgv_minimize_dev": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P], C.c_int),
     "tgvg_tgv_minimize_streaming": ([P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, P, P], C.c_int),
+    "tgvg_mlp_create": ([P, C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)], C.c_int),
+    "tgvg_mlp_destroy": ([P], C.c_int),
+    "tgvg_mlp_num_params": ([], C.c_int32),
+    "tgvg_mlp_params": ([P, P, P, P], C.c_int),
+    "tgvg_mlp_features": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, P], C.c_int),
+    "tgvg_mlp_predict": ([P, P, P, C.c_int64, P], C.c_int),
+    "tgvg_mlp_warm_start": ([P, P, P, P, C.c_int64, C.c_int32, P, C.c_int32, P], C.c_int),
+    "tgvg_mlp_warm_start_dev": ([P, P, P, P, C.c_int64, C.c_int32, P, C.c_int32, P], C.c_int),
+    "tgvg_mlp_grad": ([P, P, P, P, C.c_int64, P, P], C.c_int),
+    "tgvg_mlp_train": ([P, P, P, P, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P], C.c_int),
     "tgvg_save_tgv": ([C.c_char_p, P, C.c_int64], C.c_int),
     "tgvg_load_tgv": ([C.c_char_p, P, C.c_int64], C.c_int64),
     "tgvg_save_histograms": ([C.c_char_p, P, C.c_int64], C.c_int),

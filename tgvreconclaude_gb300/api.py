@@ -43,6 +43,14 @@ class Context:
     def stream(self) -> int:
         return self.lib.tgvg_stream(self.h) or 0
 
+    def set_graphs(self, on: bool) -> None:
+        """CUDA graphs for the level loop (default on; tgvg_set_graphs)."""
+        self.check(self.lib.tgvg_set_graphs(self.h, int(bool(on))), "tgvg_set_graphs")
+
+    def set_schedule(self, mode: str, cls: int, cfg: int) -> None:
+        """Fix the iteration schedule of a size class (tgvg_set_schedule)."""
+        self.check(self.lib.tgvg_set_schedule(self.h, MODES[mode], cls, cfg), "tgvg_set_schedule")
+
     def kernel_count(self) -> int:
         return self.lib.tgvg_kernel_count(self.h)
 

@@ -45,6 +45,7 @@ int tgvg_ctx::fail(int rc, const std::string& what) {
 
 int tgvg_ctx::cuda_fail(cudaError_t e, const char* what) {
     last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();  // a failed call also sets the runtime's last error; clear it for the next call
     return e == cudaErrorMemoryAllocation ? TGVG_ERR_NOMEM : TGVG_ERR_CUDA;
 }
 
@@ -76,10 +77,17 @@ extern "C" void tgvg_level_thresholds(float* t13) {
 }
 
 extern "C" int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg) {
-    if (!ctx || mode < 0 || mode > 2 || cls < -1 || cls > 31 || cfg < -1 || cfg > 7) return TGVG_ERR_INVALID;
+    if (!ctx || mode < 0 || mode > 2 || cls < -1 || cls > 31 || cfg < -1 || cfg > 9) return TGVG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     for (int c = 0; c < 32; ++c)
         if (cls < 0 || c == cls) ctx->tune[mode][c] = cfg;
+    return TGVG_OK;
+}
+
+extern "C" int tgvg_set_graphs(tgvg_ctx* ctx, int on) {
+    if (!ctx) return TGVG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->graphs = on != 0;
     return TGVG_OK;
 }
 
@@ -150,6 +158,7 @@ extern "C" int tgvg_destroy(tgvg_ctx* ctx) {
         for (auto& e : ctx->ev) cudaEventDestroy(e);
         for (auto& e : ctx->tev) cudaEventDestroy(e);
         for (auto& e : ctx->lev_ev) cudaEventDestroy(e);
+        if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
         cudaStreamDestroy(ctx->stream);
     }
     delete ctx;

@@ -135,7 +135,9 @@ enum BufId {
     // Stage 6
     B_T_CUBES, B_T_HISTS, B_T_UINIT, B_T_OUT, B_KEYS, B_DEPTH, B_LEAFOF, B_BUCKET, B_BCOUNT,
     B_BOFF, B_BTOT, B_PERM, B_INV, B_HKEYS, B_HMIN, B_HMAX, B_NB, B_PAR, B_UV, B_BAR, B_P4, B_Q4,
-    B_Q1, B_DAT, B_SNAP, B_LID, B_LEAVES, B_ACC, B_FLAGS, B_RANGES, B_RESID,
+    B_Q1, B_DAT, B_SNAP, B_LID, B_LEAVES, B_ACC, B_FLAGS, B_RANGES, B_RESID, B_LVSTAT,
+    // learned warm start
+    B_M_X, B_M_T, B_M_IDX, B_M_Y, B_M_LEAVES, B_M_LEAFID,
     B_COUNT
 };
 
@@ -156,6 +158,11 @@ struct tgvg_ctx {
     int coop_max[3][2] = {};           // co-resident blocks of the persistent kernel per mode / stop
     int iter_occ[3][2][2] = {};        // blocks/SM of the sweep kernels [mode][register-capped][dual, primal]
     cudaEvent_t lev_ev[2 * TGVG_MAX_LEVELS] = {};  // per-level start/end
+    bool graphs = true;                // capture the level loop into a CUDA graph when possible
+    std::vector<uint64_t> graph_key;   // problem signature of the cached graph
+    cudaGraphExec_t graph_exec = nullptr;
+    int64_t graph_kernels = 0;         // kernel nodes in the cached graph
+    bool capturing = false;            // the level loop is being captured
     tgvg_ctx() {
         for (auto& m : tune)
             for (int& c : m) c = -1;

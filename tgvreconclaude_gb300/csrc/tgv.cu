@@ -351,6 +351,7 @@ struct IterArgs {
     int* err;             // set when a bounded wait gives up
     int* iters_run;
     double* resid;
+    int pf;               // per-launch schedules: L2 prefetch of the warp's next group (0 = off)
 };
 
 // Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
@@ -516,12 +517,43 @@ __device__ __forceinline__ void primal_cube(const IterArgs& a, int p, double& dd
 // A block's share of one sweep over positions [beg, end): warps take 32-cube
 // groups in order (or in reverse order with REV, so that a sweep starts where
 // the previous one ended and finds its last writes still in L2).
+// L2 prefetch of the contiguous per-position streams of the 32-cube group at
+// position q0 (one 128-byte line per lane): the own-cube records a sweep reads,
+// so that their DRAM latency overlaps the current group's work without holding
+// registers.  The neighbour gathers are left to the caches.
+template <bool DUAL>
+__device__ __forceinline__ void prefetch_group(const IterArgs& a, int q0, int end, int lane) {
+    // every line starts at a position below `end`, so each address is inside its array
+    const void* line = nullptr;
+    const int k4 = lane & 3;        // float4 streams: line k covers positions q0 + 8k ..
+    const bool in4 = q0 + 8 * k4 < end;
+    if (DUAL) {
+        if (lane < 4) line = in4 ? a.bar + q0 + 8 * k4 : nullptr;
+        else if (lane < 8) line = in4 ? a.P4 + q0 + 8 * k4 : nullptr;
+        else if (lane < 12) line = in4 ? a.Q4 + q0 + 8 * k4 : nullptr;
+        else if (lane == 12) line = a.Q1 + q0;
+        else if (lane < 16) line = a.nb + (size_t)(2 * (lane - 13)) * a.npos + q0;
+    } else {
+        if (lane < 4) line = in4 ? a.uv + q0 + 8 * k4 : nullptr;
+        else if (lane < 8) line = in4 ? a.P4 + q0 + 8 * k4 : nullptr;
+        else if (lane < 12) line = in4 ? a.Q4 + q0 + 8 * k4 : nullptr;
+        else if (lane == 12) line = a.Q1 + q0;
+        else if (lane < 15) line = q0 + 16 * (lane - 13) < end ? a.dat + q0 + 16 * (lane - 13) : nullptr;
+        else if (lane < 18) line = a.nb + (size_t)(2 * (lane - 15) + 1) * a.npos + q0;
+    }
+    if (line && q0 < end) asm volatile("prefetch.global.L2 [%0];" ::"l"(line));
+}
+
 template <int MODE, bool RES, bool STOP, bool CG, bool DUAL, bool REV>
 __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpAcc& wa) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int ngroups = (end - beg + 31) >> 5;
     for (int gi = warp; gi < ngroups; gi += nw) {
         const int g = REV ? (ngroups - 1 - gi) : gi;
+        if (!CG && a.pf > 0 && gi + a.pf * nw < ngroups) {
+            const int gn = REV ? (ngroups - 1 - (gi + a.pf * nw)) : gi + a.pf * nw;
+            prefetch_group<DUAL>(a, beg + gn * 32, end, lane);
+        }
         const int p = beg + g * 32 + lane;
         int slot = -1;
         if (p < end) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
@@ -588,9 +620,17 @@ __device__ __forceinline__ bool grid_sync(unsigned* count, unsigned* gen, int* e
     return *(volatile int*)err == 0;
 }
 
-// Stopping test for all slots, run by block 0 between barriers (k_check's logic).
+// Stopping slots a unit owns: every leaf's slot when all leaves of a level run
+// together (streaming semantics), else its own one (the level in in-memory
+// semantics, one leaf in OC semantics, where leaves run one after another and
+// a leaf that has not run yet must not be judged on empty sums).
+template <int MODE>
+__host__ __device__ __forceinline__ int unit_slots(int nslot) { return MODE == M_STREAM ? nslot : 1; }
+
+// Stopping test of the unit's slots, run by block 0 between barriers (k_check's logic).
+template <int MODE>
 __device__ __forceinline__ void check_slots(const IterArgs& a, int it) {
-    for (int s = threadIdx.x; s < a.nslot; s += blockDim.x) {
+    for (int s = a.slot0 + threadIdx.x; s < a.slot0 + unit_slots<MODE>(a.nslot); s += blockDim.x) {
         if (a.done[s]) continue;
         double* q = a.acc + s * 4;
         const double num = sqrt(__ldcg(q + 0)) + sqrt(__ldcg(q + 1));
@@ -623,7 +663,7 @@ __global__ void __launch_bounds__(ITER_BLOCK) k_level_persistent(IterArgs a) {
         if (res) {
             wp.flush(a.acc, 0, threadIdx.x & 31);
             if (!grid_sync(a.bar_count, a.bar_gen, a.err)) return;
-            if (blockIdx.x == 0) check_slots(a, it);
+            if (blockIdx.x == 0) check_slots<MODE>(a, it);
         }
         if (!grid_sync(a.bar_count, a.bar_gen, a.err)) return;
     }
@@ -631,10 +671,10 @@ __global__ void __launch_bounds__(ITER_BLOCK) k_level_persistent(IterArgs a) {
 
 // Stopping test after a residual iteration: relative fixed-point residual
 // (|x+ - x| + |y+ - y|) / (|x+| + |y+|) in FP64 per slot (sigma = tau).
-__global__ void k_check(int nslot, double* __restrict__ acc, int* __restrict__ done, float tol, int iter,
+__global__ void k_check(int s0, int ns, double* __restrict__ acc, int* __restrict__ done, float tol, int iter,
                         int* __restrict__ iters_run, double* __restrict__ resid) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nslot || done[s]) return;
+    const int s = s0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= s0 + ns || done[s]) return;
     double* q = acc + s * 4;
     const double num = sqrt(q[0]) + sqrt(q[1]);
     const double den = sqrt(q[2]) + sqrt(q[3]);
@@ -705,9 +745,12 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 // Every schedule applies the identical per-cube arithmetic, so the choice never
 // changes a result, only the time.
 // cfg 7 (CFG_LEAN): as cfg 0 with the sweep kernels capped at 32 registers.
+// cfg 8 / 9: as cfg 0 / 7 with an L2 prefetch of each warp's next group.
 static constexpr int TUNE_SEG = 16;
 static constexpr int N_PERSIST_CFG = 6;
 static constexpr int CFG_LEAN = 7;
+static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
+static inline bool per_launch_cfg(int cfg) { return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF; }
 
 static int persist_grid(int n, int cfg, int cmax) {
     const int cpb = 256 << cfg;
@@ -730,25 +773,38 @@ static int coop_capacity(tgvg_ctx* ctx, bool stop, int* out) {
     return TGVG_OK;
 }
 
+// An event record: inside a stream capture it becomes an event record node of
+// the graph (so graph replays are timed too); outside, a plain record.
+static cudaError_t record_event(cudaEvent_t e, cudaStream_t s, bool capturing) {
+    return capturing ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s);
+}
+
+// Per-launch timing samples every TIMING_STRIDE-th iteration of the timed level.
+static constexpr int TIMING_STRIDE = 10;
+
 template <int MODE>
 static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, bool stop, bool timed) {
     if (count <= 0) return TGVG_OK;
-    if (cfg == 0 || cfg == CFG_LEAN) {
-        const bool lean = cfg == CFG_LEAN;
+    if (per_launch_cfg(cfg)) {
+        const bool lean = cfg == CFG_LEAN || cfg == CFG_LEAN_PF;
+        a.pf = (cfg == CFG_PF || cfg == CFG_LEAN_PF) ? 1 : 0;
         int rc = iter_occupancy<MODE>(ctx);
         if (rc) return rc;
         for (int it = it0; it < it0 + count; ++it) {
             const bool res = stop && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
-            if (timed) cudaEventRecord(ctx->tev[3 * it], ctx->stream);
+            const bool mark = timed && it % TIMING_STRIDE == 0;
+            cudaEvent_t* te = mark ? &ctx->tev[3 * (it / TIMING_STRIDE)] : nullptr;
+            if (mark) TGVG_CK(ctx, record_event(te[0], ctx->stream, ctx->capturing));
             launch_iter<MODE>(ctx, a, res, stop, true, lean);
-            if (timed) cudaEventRecord(ctx->tev[3 * it + 1], ctx->stream);
+            if (mark) TGVG_CK(ctx, record_event(te[1], ctx->stream, ctx->capturing));
             launch_iter<MODE>(ctx, a, res, stop, false, lean);
-            if (timed) cudaEventRecord(ctx->tev[3 * it + 2], ctx->stream);
+            if (mark) TGVG_CK(ctx, record_event(te[2], ctx->stream, ctx->capturing));
             cudaError_t le = cudaGetLastError();
             if (le != cudaSuccess) return ctx->cuda_fail(le, "iteration launch");
             ctx->kernels += 2;
             if (res) {
-                k_check<<<blocks_for(a.nslot, 128), 128, 0, ctx->stream>>>(a.nslot, a.acc, a.done, a.tol, it,
+                const int ns = unit_slots<MODE>(a.nslot);
+                k_check<<<blocks_for(ns, 128), 128, 0, ctx->stream>>>(a.slot0, ns, a.acc, a.done, a.tol, it,
                                                                           a.iters_run, a.resid);
                 TGVG_LAUNCHED(ctx);
             }
@@ -773,58 +829,89 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
     return TGVG_OK;
 }
 
-// Run `iters` iterations of one unit.  The schedule for the unit's size class
-// (floor(log2 n)) is taken from the context's table; the first time a class
-// is met in a fixed-count solve with enough iterations, its first segments
-// try each candidate schedule for TUNE_SEG iterations and keep the fastest
-// (online autotuning: the tried iterations count toward the solve).
+// Candidate schedules the autotuner times for a unit of n cubes: the two
+// per-iteration-launch variants and every persistent cfg whose grid differs.
 template <int MODE>
-static int run_unit_t(tgvg_ctx* ctx, IterArgs& a, int iters, bool stop, bool timed, int* used) {
-    const int cls = 31 - __builtin_clz((unsigned)std::max(1, a.n));
-    int& tuned = ctx->tune[MODE][cls];
-    int it = 0, cfg;
-    if (timed) {
-        cfg = 0;  // per-launch event timing needs the per-sweep launches
-    } else if (tuned >= 0) {
-        cfg = tuned;
-    } else {
-        int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
-        if (rc) return rc;
-        std::vector<int> cands = {0, CFG_LEAN};
-        int last_grid = -1;
-        if (a.n <= (1 << 22))
-            for (int k = 1; k <= N_PERSIST_CFG; ++k) {
-                const int g = persist_grid(a.n, k, cmax);
-                if (g != last_grid) cands.push_back(k);
-                last_grid = g;
-            }
-        if (!stop && (int)cands.size() * TUNE_SEG * 2 <= iters) {
-            float best_ms = 1e30f;
-            int best = 0;
-            for (int c : cands) {
-                TGVG_CK(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
-                if ((rc = run_segment<MODE>(ctx, a, c, it, TUNE_SEG, stop, false))) return rc;
-                TGVG_CK(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
-                TGVG_CK(ctx, cudaEventSynchronize(ctx->ev[3]));
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
-                if (ms < best_ms) { best_ms = ms; best = c; }
-                it += TUNE_SEG;
-            }
-            tuned = best;
-            cfg = best;
-        } else {
-            cfg = a.n <= 65536 ? 3 : 0;  // untuned default: one cooperative launch for small units
+static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& cands) {
+    int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
+    if (rc) return rc;
+    cands = {0, CFG_LEAN, CFG_PF, CFG_LEAN_PF};
+    int last_grid = -1;
+    if (n <= (1 << 22))
+        for (int k = 1; k <= N_PERSIST_CFG; ++k) {
+            const int g = persist_grid(n, k, cmax);
+            if (g != last_grid) cands.push_back(k);
+            last_grid = g;
         }
+    return TGVG_OK;
+}
+
+// The schedule a unit of n cubes runs with, or -1 when the online autotuner
+// will first time the candidates on it.  The schedule for the unit's size
+// class (floor(log2 n)) is taken from the context's table; the first time a
+// class is met in a fixed-count solve with enough iterations, its first
+// segments try each candidate for TUNE_SEG iterations and keep the fastest
+// (the tried iterations count toward the solve).  Also makes sure the
+// occupancy figures the launches need are cached.
+template <int MODE>
+static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed, int* cfg) {
+    int rc = iter_occupancy<MODE>(ctx), cmax = 0;
+    if (!rc) rc = coop_capacity<MODE>(ctx, stop, &cmax);
+    if (rc) return rc;
+    const int tuned = ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, n))];
+    if (timed) {  // per-launch event timing needs one of the per-sweep-launch schedules
+        *cfg = per_launch_cfg(tuned) ? tuned : 0;
+        return TGVG_OK;
+    }
+    if (tuned >= 0) { *cfg = tuned; return TGVG_OK; }
+    std::vector<int> cands;
+    if ((rc = tune_candidates<MODE>(ctx, n, stop, cands))) return rc;
+    if (!stop && (int)cands.size() * TUNE_SEG * 2 <= iters) { *cfg = -1; return TGVG_OK; }
+    *cfg = n <= 65536 ? 3 : 0;  // untuned default: one cooperative launch for small units
+    return TGVG_OK;
+}
+
+// Run `iters` iterations of one unit with schedule `cfg` (-1: autotune first).
+template <int MODE>
+static int run_unit_t(tgvg_ctx* ctx, IterArgs& a, int iters, bool stop, bool timed, int cfg, int* used) {
+    int it = 0, rc;
+    if (cfg < 0) {
+        std::vector<int> cands;
+        if ((rc = tune_candidates<MODE>(ctx, a.n, stop, cands))) return rc;
+        float best_ms = 1e30f;
+        int best = 0;
+        for (int c : cands) {
+            TGVG_CK(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+            if ((rc = run_segment<MODE>(ctx, a, c, it, TUNE_SEG, stop, false))) return rc;
+            TGVG_CK(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+            TGVG_CK(ctx, cudaEventSynchronize(ctx->ev[3]));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+            if (ms < best_ms) { best_ms = ms; best = c; }
+            it += TUNE_SEG;
+        }
+        ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, a.n))] = best;
+        cfg = best;
     }
     *used = cfg;
     return run_segment<MODE>(ctx, a, cfg, it, iters - it, stop, timed);
 }
 
-static int run_unit(tgvg_ctx* ctx, int mode, IterArgs& a, int iters, bool stop, bool timed, int* used) {
-    if (mode == M_INMEM) return run_unit_t<M_INMEM>(ctx, a, iters, stop, timed, used);
-    if (mode == M_OC) return run_unit_t<M_OC>(ctx, a, iters, stop, timed, used);
-    return run_unit_t<M_STREAM>(ctx, a, iters, stop, timed, used);
+static int plan_unit(tgvg_ctx* ctx, int mode, int n, int iters, bool stop, bool timed, int* cfg) {
+    if (mode == M_INMEM) return plan_schedule<M_INMEM>(ctx, n, iters, stop, timed, cfg);
+    if (mode == M_OC) return plan_schedule<M_OC>(ctx, n, iters, stop, timed, cfg);
+    return plan_schedule<M_STREAM>(ctx, n, iters, stop, timed, cfg);
+}
+
+static int run_unit(tgvg_ctx* ctx, int mode, IterArgs& a, int iters, bool stop, bool timed, int cfg, int* used) {
+    if (mode == M_INMEM) return run_unit_t<M_INMEM>(ctx, a, iters, stop, timed, cfg, used);
+    if (mode == M_OC) return run_unit_t<M_OC>(ctx, a, iters, stop, timed, cfg, used);
+    return run_unit_t<M_STREAM>(ctx, a, iters, stop, timed, cfg, used);
+}
+
+__global__ void k_fill_i32(int n, int* __restrict__ p, int v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
 }
 
 int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists, int64_t n64,
@@ -991,8 +1078,6 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     const int iters = std::max(0, prm->iters);
     st.min_depth = min_d;
     st.max_depth = max_d;
-    std::vector<int> h_iters(nslot);
-    std::vector<double> h_res(nslot);
     // optional per-launch timing of the largest level (not for sequential OC leaves)
     int big_level = -1, t_level = -1;
     {
@@ -1002,110 +1087,216 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     }
     if (ctx->timing && mode != M_OC && iters > 0) {
         t_level = big_level;
-        while ((int)ctx->tev.size() < 3 * iters) {
+        while ((int)ctx->tev.size() < 3 * ((iters + TIMING_STRIDE - 1) / TIMING_STRIDE)) {
             cudaEvent_t e;
             TGVG_CK(ctx, cudaEventCreate(&e));
             ctx->tev.push_back(e);
         }
     }
+    // Plan: the levels, their launch units (INMEM / STREAM the whole level, OC
+    // one per leaf in caller order) and each unit's schedule.
+    struct Unit { int slot, o, n, cfg; };
+    struct Level { int d, o, cnt; std::vector<Unit> us; };
+    std::vector<Level> levels;
+    bool tuning = false;
     for (int Ld = min_d; Ld <= max_d; ++Ld) {
         const int o = h_bstart[Ld], cnt = h_bstart[Ld + 1] - h_bstart[Ld];
         if (cnt <= 0) continue;
-        const int slot = st.n_levels;
-        if (slot < TGVG_MAX_LEVELS) cudaEventRecord(ctx->lev_ev[2 * slot], ctx->stream);
-        int used_cfg = -1;
-        if (Ld > min_d) {
-            k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, par, prm->keep_init_u ? 1 : 0, uv,
-                                                                          bar, P4, Q4, Q1);
-            TGVG_LAUNCHED(ctx);
-        }
-        if (mode == M_STREAM) {
-            k_stream_snapshot<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, uv, bar, snap);
-            TGVG_LAUNCHED(ctx);
-        } else if (mode == M_OC) {
-            k_copy4<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, bar, snap);
-            TGVG_LAUNCHED(ctx);
-        }
-        // launch units: INMEM / STREAM the whole level; OC one per leaf, in caller order
-        struct Unit { int slot, o, n; };
-        std::vector<Unit> us;
+        Level lvl{Ld, o, cnt, {}};
         if (mode == M_OC) {
             for (int l = 0; l < L; ++l) {
                 const int a0 = h_ranges[(l * NBUCKET + Ld) * 2], a1 = h_ranges[(l * NBUCKET + Ld) * 2 + 1];
-                if (a1 > a0) us.push_back({l, a0, a1 - a0});
+                if (a1 > a0) lvl.us.push_back({l, a0, a1 - a0, 0});
             }
         } else {
-            us.push_back({0, o, cnt});
+            lvl.us.push_back({0, o, cnt, 0});
         }
-        if (stop) {
-            TGVG_CK(ctx, cudaMemsetAsync(acc, 0, 32ull * nslot, ctx->stream));
-            TGVG_CK(ctx, cudaMemsetAsync(done, 0, 4ull * nslot, ctx->stream));
-            std::vector<int> full(nslot, iters);
-            TGVG_CK(ctx, cudaMemcpyAsync(iters_run, full.data(), 4ull * nslot, cudaMemcpyHostToDevice,
-                                         ctx->stream));
-            TGVG_CK(ctx, cudaMemsetAsync(resid, 0, 8ull * nslot, ctx->stream));
-        }
-        // NVTX range per level so profilers can select the largest level's launches
-        nvtxRangePushA(Ld == big_level ? "tgv_largest_level" : "tgv_level");
-        for (const Unit& u : us) {
-            IterArgs a;
-            std::memset(&a, 0, sizeof(a));
-            a.o = u.o; a.n = u.n; a.npos = n;
-            a.nb = nb; a.uv = uv; a.bar = bar; a.P4 = P4; a.Q4 = Q4; a.Q1 = Q1; a.dat = dat; a.snap = snap;
-            a.lid = lid; a.acc = acc; a.done = done; a.slot0 = u.slot;
-            a.alpha0 = prm->alpha0; a.alpha1 = prm->alpha1;
-            a.check_every = std::max(1, prm->check_every); a.nslot = nslot; a.tol = prm->tol; a.iters_total = iters;
-            a.bar_count = reinterpret_cast<unsigned*>(flags + 4);
-            a.bar_gen = reinterpret_cast<unsigned*>(flags + 5);
-            a.err = flags + 6;
-            a.iters_run = iters_run; a.resid = resid;
-            const int rc = run_unit(ctx, mode, a, iters, stop, Ld == t_level, &used_cfg);
+        for (Unit& u : lvl.us) {
+            const int rc = plan_unit(ctx, mode, u.n, iters, stop, Ld == t_level, &u.cfg);
             if (rc) return rc;
+            tuning |= u.cfg < 0;
         }
-        nvtxRangePop();
-        if (slot < TGVG_MAX_LEVELS) cudaEventRecord(ctx->lev_ev[2 * slot + 1], ctx->stream);
-        // level stats
-        if (st.n_levels < TGVG_MAX_LEVELS) {
-            const int k = st.n_levels++;
-            st.schedule[k] = used_cfg;
-            st.depth[k] = Ld;
-            st.active[k] = cnt;
+        levels.push_back(std::move(lvl));
+    }
+    const int nlv = std::min<int>((int)levels.size(), TGVG_MAX_LEVELS);
+    double* lv_res = nullptr;
+    int* lv_it = nullptr;
+    if (stop) {
+        auto* lvstat = (double*)B(B_LVSTAT, 12ull * TGVG_MAX_LEVELS * nslot);
+        if (!lvstat) return TGVG_ERR_NOMEM;
+        lv_res = lvstat;
+        lv_it = reinterpret_cast<int*>(lvstat + TGVG_MAX_LEVELS * nslot);
+    }
+    std::vector<int> used(nlv, -1);
+
+    // Enqueue every level.  Device-only work: stopping flags and per-level
+    // iteration counts / residuals stay on the device (copied per level into
+    // lv_it / lv_res) and are read once after the loop, so the sequence can be
+    // captured into a CUDA graph.
+    auto enqueue = [&](bool capturing) -> int {
+        for (int k = 0; k < (int)levels.size(); ++k) {
+            const Level& lvl = levels[k];
+            const int Ld = lvl.d, o = lvl.o, cnt = lvl.cnt;
+            if (k < TGVG_MAX_LEVELS)
+                TGVG_CK(ctx, record_event(ctx->lev_ev[2 * k], ctx->stream, capturing));
+            if (Ld > min_d) {
+                k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, par, prm->keep_init_u ? 1 : 0,
+                                                                              uv, bar, P4, Q4, Q1);
+                TGVG_LAUNCHED(ctx);
+            }
+            if (mode == M_STREAM) {
+                k_stream_snapshot<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, uv, bar, snap);
+                TGVG_LAUNCHED(ctx);
+            } else if (mode == M_OC) {
+                k_copy4<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, bar, snap);
+                TGVG_LAUNCHED(ctx);
+            }
             if (stop) {
-                TGVG_CK(ctx, cudaMemcpyAsync(h_iters.data(), iters_run, 4ull * nslot, cudaMemcpyDeviceToHost,
-                                             ctx->stream));
-                TGVG_CK(ctx, cudaMemcpyAsync(h_res.data(), resid, 8ull * nslot, cudaMemcpyDeviceToHost,
-                                             ctx->stream));
-                TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
-                int itmax = 0;
-                double rmax = 0.0;
-                int64_t li = 0;
-                if (mode == M_INMEM) {
-                    itmax = h_iters[0]; rmax = h_res[0]; li = int64_t(cnt) * itmax;
-                } else {
-                    for (int l = 0; l < L; ++l) {
-                        const int a0 = h_ranges[(l * NBUCKET + Ld) * 2], a1 = h_ranges[(l * NBUCKET + Ld) * 2 + 1];
-                        if (a1 <= a0) continue;
-                        itmax = std::max(itmax, h_iters[l]);
-                        rmax = std::max(rmax, h_res[l]);
-                        li += int64_t(a1 - a0) * h_iters[l];
-                    }
+                TGVG_CK(ctx, cudaMemsetAsync(acc, 0, 32ull * nslot, ctx->stream));
+                TGVG_CK(ctx, cudaMemsetAsync(done, 0, 4ull * nslot, ctx->stream));
+                k_fill_i32<<<blocks_for(nslot, 128), 128, 0, ctx->stream>>>(nslot, iters_run, iters);
+                TGVG_LAUNCHED(ctx);
+                TGVG_CK(ctx, cudaMemsetAsync(resid, 0, 8ull * nslot, ctx->stream));
+            }
+            // NVTX range per level so profilers can select the largest level's launches
+            nvtxRangePushA(Ld == big_level ? "tgv_largest_level" : "tgv_level");
+            int used_cfg = -1;
+            for (const Unit& u : lvl.us) {
+                IterArgs a;
+                std::memset(&a, 0, sizeof(a));
+                a.o = u.o; a.n = u.n; a.npos = n;
+                a.nb = nb; a.uv = uv; a.bar = bar; a.P4 = P4; a.Q4 = Q4; a.Q1 = Q1; a.dat = dat; a.snap = snap;
+                a.lid = lid; a.acc = acc; a.done = done; a.slot0 = u.slot;
+                a.alpha0 = prm->alpha0; a.alpha1 = prm->alpha1;
+                a.check_every = std::max(1, prm->check_every); a.nslot = nslot; a.tol = prm->tol;
+                a.iters_total = iters;
+                a.bar_count = reinterpret_cast<unsigned*>(flags + 4);
+                a.bar_gen = reinterpret_cast<unsigned*>(flags + 5);
+                a.err = flags + 6;
+                a.iters_run = iters_run; a.resid = resid;
+                const int rc = run_unit(ctx, mode, a, iters, stop, Ld == t_level, u.cfg, &used_cfg);
+                if (rc) { nvtxRangePop(); return rc; }
+            }
+            nvtxRangePop();
+            if (k < TGVG_MAX_LEVELS) {
+                used[k] = used_cfg;
+                TGVG_CK(ctx, record_event(ctx->lev_ev[2 * k + 1], ctx->stream, capturing));
+                if (stop) {
+                    TGVG_CK(ctx, cudaMemcpyAsync(lv_it + k * nslot, iters_run, 4ull * nslot,
+                                                 cudaMemcpyDeviceToDevice, ctx->stream));
+                    TGVG_CK(ctx, cudaMemcpyAsync(lv_res + k * nslot, resid, 8ull * nslot,
+                                                 cudaMemcpyDeviceToDevice, ctx->stream));
                 }
-                st.iters_run[k] = itmax;
-                st.residual[k] = rmax;
-                st.leaf_iters += li;
-            } else {
-                st.iters_run[k] = iters;
-                st.leaf_iters += int64_t(cnt) * iters;
             }
         }
+        return TGVG_OK;
+    };
+
+    if (ctx->graphs && !tuning && !levels.empty()) {
+        // Problem signature: everything the captured launches bake in.
+        std::vector<uint64_t> key = {
+            (uint64_t)mode, (uint64_t)n, (uint64_t)nslot, (uint64_t)iters, (uint64_t)stop,
+            (uint64_t)std::max(1, prm->check_every), (uint64_t)(prm->keep_init_u ? 1 : 0), (uint64_t)min_d,
+            (uint64_t)(t_level + 1)};
+        uint32_t fb[3];
+        std::memcpy(&fb[0], &prm->alpha0, 4);
+        std::memcpy(&fb[1], &prm->alpha1, 4);
+        std::memcpy(&fb[2], &prm->tol, 4);
+        for (uint32_t f : fb) key.push_back(f);
+        const void* ptrs[] = {nb, par, uv, bar, P4, Q4, Q1, dat, snap, lid, acc, flags, resid, lv_res};
+        for (const void* q : ptrs) key.push_back((uint64_t)(uintptr_t)q);
+        for (const Level& lvl : levels) {
+            key.push_back(((uint64_t)lvl.d << 32) | (uint32_t)lvl.o);
+            key.push_back((uint64_t)lvl.cnt);
+            for (const Unit& u : lvl.us) {
+                key.push_back(((uint64_t)u.slot << 32) | (uint32_t)u.o);
+                key.push_back(((uint64_t)u.n << 8) | (uint32_t)u.cfg);
+            }
+        }
+        if (ctx->graph_exec && key == ctx->graph_key) {
+            TGVG_CK(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+            ctx->kernels += ctx->graph_kernels;
+            for (int k = 0; k < nlv; ++k) used[k] = levels[k].us.empty() ? -1 : levels[k].us.back().cfg;
+            st.graph = 2;
+        } else {
+            if (ctx->graph_exec) {
+                cudaGraphExecDestroy(ctx->graph_exec);
+                ctx->graph_exec = nullptr;
+                ctx->graph_key.clear();
+            }
+            const int64_t kbefore = ctx->kernels;
+            TGVG_CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            ctx->capturing = true;
+            const int rc = enqueue(true);
+            ctx->capturing = false;
+            cudaGraph_t g = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+            if (rc || ce != cudaSuccess || !g) {
+                if (g) cudaGraphDestroy(g);
+                return rc ? rc : ctx->cuda_fail(ce, "level loop capture");
+            }
+            cudaGraphExec_t ex = nullptr;
+            const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) return ctx->cuda_fail(ie, "level loop graph instantiate");
+            ctx->graph_exec = ex;
+            ctx->graph_key = std::move(key);
+            ctx->graph_kernels = ctx->kernels - kbefore;
+            TGVG_CK(ctx, cudaGraphLaunch(ex, ctx->stream));
+            st.graph = 1;
+        }
+    } else {
+        const int rc = enqueue(false);
+        if (rc) return rc;
     }
+
     TGVG_CK(ctx, cudaEventRecord(e2, ctx->stream));
     k_unpermute<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, inv, uv, P4, Q4, Q1, reinterpret_cast<float*>(d_out));
     TGVG_LAUNCHED(ctx);
+    // level stats
+    std::vector<int> h_it;
+    std::vector<double> h_rs;
+    if (stop && nlv > 0) {
+        h_it.resize((size_t)nlv * nslot);
+        h_rs.resize((size_t)nlv * nslot);
+        TGVG_CK(ctx, cudaMemcpyAsync(h_it.data(), lv_it, 4ull * nlv * nslot, cudaMemcpyDeviceToHost, ctx->stream));
+        TGVG_CK(ctx, cudaMemcpyAsync(h_rs.data(), lv_res, 8ull * nlv * nslot, cudaMemcpyDeviceToHost, ctx->stream));
+    }
     int h_err = 0;
     TGVG_CK(ctx, cudaMemcpyAsync(&h_err, flags + 6, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (h_err) return ctx->fail(TGVG_ERR_TIMEOUT, "a grid barrier of the persistent iteration kernel timed out");
+    for (int k = 0; k < nlv; ++k) {
+        const Level& lvl = levels[k];
+        st.n_levels = k + 1;
+        st.schedule[k] = used[k];
+        st.depth[k] = lvl.d;
+        st.active[k] = lvl.cnt;
+        if (stop) {
+            const int* it_k = h_it.data() + (size_t)k * nslot;
+            const double* rs_k = h_rs.data() + (size_t)k * nslot;
+            int itmax = 0;
+            double rmax = 0.0;
+            int64_t li = 0;
+            if (mode == M_INMEM) {
+                itmax = it_k[0]; rmax = rs_k[0]; li = int64_t(lvl.cnt) * itmax;
+            } else {  // one stopping slot per leaf
+                for (int l = 0; l < L; ++l) {
+                    const int a0 = h_ranges[(l * NBUCKET + lvl.d) * 2], a1 = h_ranges[(l * NBUCKET + lvl.d) * 2 + 1];
+                    if (a1 <= a0) continue;
+                    itmax = std::max(itmax, it_k[l]);
+                    rmax = std::max(rmax, rs_k[l]);
+                    li += int64_t(a1 - a0) * it_k[l];
+                }
+            }
+            st.iters_run[k] = itmax;
+            st.residual[k] = rmax;
+            st.leaf_iters += li;
+        } else {
+            st.iters_run[k] = iters;
+            st.leaf_iters += int64_t(lvl.cnt) * iters;
+        }
+    }
     float ms_setup = 0.f, ms_iter = 0.f;
     cudaEventElapsedTime(&ms_setup, e0, e1);
     cudaEventElapsedTime(&ms_iter, e1, e2);
@@ -1120,15 +1311,16 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     }
     if (t_level >= 0) {
         double dsum = 0.0, psum = 0.0;
-        for (int it = 0; it < iters; ++it) {
+        const int nt = (iters + TIMING_STRIDE - 1) / TIMING_STRIDE;
+        for (int k = 0; k < nt; ++k) {
             float a = 0.f, b = 0.f;
-            cudaEventElapsedTime(&a, ctx->tev[3 * it], ctx->tev[3 * it + 1]);
-            cudaEventElapsedTime(&b, ctx->tev[3 * it + 1], ctx->tev[3 * it + 2]);
+            cudaEventElapsedTime(&a, ctx->tev[3 * k], ctx->tev[3 * k + 1]);
+            cudaEventElapsedTime(&b, ctx->tev[3 * k + 1], ctx->tev[3 * k + 2]);
             dsum += a;
             psum += b;
         }
         st.kt_depth = t_level;
-        st.kt_launches = iters;
+        st.kt_launches = nt;
         st.kt_active = h_bstart[t_level + 1] - h_bstart[t_level];
         st.kt_dual_ms = dsum;
         st.kt_primal_ms = psum;

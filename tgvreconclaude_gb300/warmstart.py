@@ -1,0 +1,227 @@
+"""Learned warm start for the TGV solve.
+
+A per-cube MLP (F -> 64 -> 64 -> 1, F = nbins + 5 features: the histogram
+normalised by its total, depth / 21, the cube centre's position inside its
+chunk's node, and the median indicator) predicts the converged u minus the
+median indicator, the reference's own start; the warm start is median +
+network.  It is trained on the GPU by this package's own forward/backward
+kernels (include/tgvg.h, tgvg_mlp_*) on pairs that the plain solver produces
+on seeded scenes, and it seeds a solve with params.init = "given" and
+keep_init_u = True: every level starts from the prediction instead of the
+parent's u.  The plain primal-dual iterations still run to the same stopping
+tolerance, so the prediction only changes how many iterations that takes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N, api, formats as F, scenes as S, workloads as W
+
+
+class WarmStartMLP:
+    def __init__(self, nbins: int = 10, seed: int = 0):
+        self.ctx = api.context()
+        self.lib = self.ctx.lib
+        h = C.c_void_p()
+        self.ctx.check(self.lib.tgvg_mlp_create(self.ctx.h, nbins, seed, C.byref(h)), "tgvg_mlp_create")
+        self.h = h
+        self.nbins = nbins
+        self.n_params = self.lib.tgvg_mlp_num_params()
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.tgvg_mlp_destroy(self.h)
+        except Exception:
+            pass
+
+    # -- parameters
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, np.float32)
+        self.ctx.check(self.lib.tgvg_mlp_params(self.ctx.h, self.h, p.ctypes.data, None), "mlp params")
+        return p
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        self.ctx.check(self.lib.tgvg_mlp_params(self.ctx.h, self.h, None, p.ctypes.data), "mlp params")
+
+    def save(self, path) -> None:
+        np.savez(path, params=self.get_params(), nbins=self.nbins)
+
+    @classmethod
+    def load(cls, path) -> "WarmStartMLP":
+        d = np.load(path)
+        m = cls(int(d["nbins"]))
+        m.set_params(d["params"])
+        return m
+
+    # -- data
+    def features(self, cubes, hists, leaves=None) -> np.ndarray:
+        cubes = np.ascontiguousarray(cubes, F.CUBE_DTYPE)
+        hists = np.ascontiguousarray(hists, np.uint32)
+        X = np.zeros((len(cubes), 16), np.uint16)
+        lv = None if leaves is None else np.ascontiguousarray(leaves, F.LEAF_DTYPE)
+        self.ctx.check(self.lib.tgvg_mlp_features(self.ctx.h, api._p(cubes), api._p(hists), len(cubes),
+                                                  hists.shape[1], api._p(lv), 0 if lv is None else len(lv),
+                                                  api._p(X)), "tgvg_mlp_features")
+        return X
+
+    def predict(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.uint16)
+        y = np.zeros(len(X), np.float32)
+        self.ctx.check(self.lib.tgvg_mlp_predict(self.ctx.h, self.h, api._p(X), len(X), api._p(y)),
+                       "tgvg_mlp_predict")
+        return y
+
+    def warm_start(self, cubes, hists, leaves=None) -> np.ndarray:
+        """u = median indicator + network, computed on the device."""
+        cubes = np.ascontiguousarray(cubes, F.CUBE_DTYPE)
+        hists = np.ascontiguousarray(hists, np.uint32)
+        lv = None if leaves is None else np.ascontiguousarray(leaves, F.LEAF_DTYPE)
+        u = np.zeros(len(cubes), np.float32)
+        self.ctx.check(self.lib.tgvg_mlp_warm_start(self.ctx.h, self.h, api._p(cubes), api._p(hists), len(cubes),
+                                                    hists.shape[1], api._p(lv), 0 if lv is None else len(lv),
+                                                    api._p(u)), "tgvg_mlp_warm_start")
+        return u
+
+    def grad(self, X, t):
+        X = np.ascontiguousarray(X, np.uint16)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_float()
+        self.ctx.check(self.lib.tgvg_mlp_grad(self.ctx.h, self.h, api._p(X), api._p(t), len(X), api._p(g),
+                                              C.byref(loss)), "tgvg_mlp_grad")
+        return loss.value, g
+
+    def train(self, X, t, epochs: int = 10, batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> float:
+        X = np.ascontiguousarray(X, np.uint16)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = C.c_float()
+        self.ctx.check(self.lib.tgvg_mlp_train(self.ctx.h, self.h, api._p(X), api._p(t), len(X), epochs, batch,
+                                               C.c_float(lr), seed, C.byref(loss)), "tgvg_mlp_train")
+        return loss.value
+
+
+# ------------------------------------------------------------ scene data ---
+
+SMALL = dict(torus=dict(scene="torus", ncam=16, cam_radius=4.0, width=320, height=240, half_fov=25.0,
+                        origin=(-1.5, -1.5, -1.5), r_root=1.5, max_depth=7, nbins=10),
+             three=dict(scene="three", ncam=16, cam_radius=6.5, width=320, height=240, half_fov=28.0,
+                        origin=(-3.0, -3.0, -3.0), r_root=3.0, max_depth=8, nbins=10))
+
+
+def small_scene(seed: int, kind: str = "torus", device: str = "cuda"):
+    """A reduced scene of the torus / three-object configurations: 16 cameras at
+    320x240, cubes to depth 7 (torus) or 8 (three objects).  The cameras stand
+    far enough out (radius 4 / 6.5) that each sees the whole object: with closer
+    or fewer cameras a quarter of the finest cubes get at most two votes, and on
+    those the reference iteration is unstable (u grows by up to ~0.75 per
+    iteration without bound)."""
+    import torch
+    cfg = SMALL[kind]
+    rng = np.random.default_rng(seed)
+    scene = W.make_scene(cfg["scene"], rng)
+    if kind == "torus":  # vary the torus per seed
+        scene[0]["R"] = float(rng.uniform(0.8, 1.1))
+        scene[0]["r"] = float(rng.uniform(0.2, 0.35))
+        scene[0]["sigma"] = float(rng.uniform(0.002, 0.008))
+    rig = S.sphere_rig(cfg["ncam"], cfg["cam_radius"] * float(rng.uniform(0.9, 1.1)), width=cfg["width"],
+                       height=cfg["height"], half_fov_deg=cfg["half_fov"])
+    Ps, Rs, depths, cams = [], [], [], []
+    for i, c in enumerate(rig):
+        d = S.render_depth(scene, c, seed=seed * 1000 + i, device=device, dtype=torch.float32, steps=128)
+        P, r = S.samples_from_depth_map(d, c, torch)
+        Ps.append(P); Rs.append(r); depths.append(d.cpu().numpy()); cams.append(W.camera(c))
+    key, rc = S.cubes_from_samples(torch.cat(Ps), torch.cat(Rs), cfg["origin"], cfg["r_root"], cfg["max_depth"],
+                                   torch)
+    key, rc = S.balance_2to1(key, rc, cfg["r_root"], torch)
+    cubes = S.keys_to_cubes(key, rc)
+    hists = api.compute_histograms_from_maps(cubes, cams, depths, cfg["origin"], cfg["r_root"], cfg["nbins"])
+    return cubes, hists
+
+
+SOLVE = dict(alpha0=2.0, alpha1=1.0)
+
+
+def converged_u(cubes, hists, tol: float = 1e-6, max_iters: int = 6000):
+    """Plain solver (reference initialisation) run to a tight residual."""
+    prm = api.TGVParams(alpha0=SOLVE["alpha0"], alpha1=SOLVE["alpha1"], iters=max_iters, tol=tol, check_every=20)
+    out, st = api.tgv_solve(cubes, hists, None, "inmem", prm)
+    return out["u"].copy(), st
+
+
+# Cubes whose solved |u| exceeds this have no fixed point of the reference
+# iteration (weakly observed cubes on which u drifts without bound); they are
+# left out of the training pairs.
+U_BOUND = 1.5
+
+
+def dataset(seeds, kinds=("torus", "three")):
+    """Training pairs: features and converged u minus the median indicator,
+    over the cubes whose converged |u| <= U_BOUND."""
+    Xs, ts = [], []
+    mlp = WarmStartMLP()
+    for s in seeds:
+        kind = kinds[s % len(kinds)]
+        cubes, hists = small_scene(s, kind)
+        u, _ = converged_u(cubes, hists)
+        ok = np.abs(u) <= U_BOUND
+        Xs.append(mlp.features(cubes, hists)[ok])
+        ts.append((u - median_start(hists))[ok])
+    return np.concatenate(Xs), np.concatenate(ts)
+
+
+@dataclass
+class SolveRecord:
+    leaf_iters: int
+    iters: list
+    device_ms: float
+    wall_ms: float
+    predict_ms: float = 0.0
+
+
+def time_to_tol(cubes, hists, u0=None, tol: float = 1e-4, max_iters: int = 6000, check_every: int = 10):
+    """Solve to relative residual `tol` from a zero start (u0 None) or from u0,
+    every level keeping its initial u.  Returns a SolveRecord."""
+    init = "zero" if u0 is None else "given"
+    prm = api.TGVParams(alpha0=SOLVE["alpha0"], alpha1=SOLVE["alpha1"], iters=max_iters, tol=tol,
+                        check_every=check_every, init=init, keep_init_u=True)
+    t0 = time.perf_counter()
+    out, st = api.tgv_solve(cubes, hists, None, "inmem", prm, u_init=u0)
+    wall = 1e3 * (time.perf_counter() - t0)
+    return out, SolveRecord(st["leaf_iters"], st["iters_run"], st["total_ms"], wall)
+
+
+def median_start(hists) -> np.ndarray:
+    """The reference's initial u: the histogram's median indicator, 0 when empty
+    (src/histogram.cpp:12-31)."""
+    h = np.asarray(hists, np.uint32)
+    nb = h.shape[1]
+    tot = h.sum(1, dtype=np.uint32)
+    k = np.argmax(np.cumsum(h, 1, dtype=np.uint32) * np.uint32(2) >= tot[:, None], axis=1)
+    med = np.float32(-1.0) + (k.astype(np.float32) + np.float32(0.5)) / np.float32(nb / 2.0)
+    return np.where(tot > 0, med, np.float32(0.0)).astype(np.float32)
+
+
+def start_errors(mlp: WarmStartMLP, cubes, hists, u_conv) -> dict:
+    """RMS distance to the converged u of the three starts: zero, the median
+    indicator, and the network's prediction."""
+    pred = mlp.warm_start(cubes, hists)
+    rms = lambda a: float(np.sqrt(np.mean((np.asarray(a, np.float64) - u_conv) ** 2)))
+    return dict(zero=rms(np.zeros_like(u_conv)), median=rms(median_start(hists)), network=rms(pred))
+
+
+def compare(mlp: WarmStartMLP, cubes, hists, tol: float = 1e-4):
+    """Zero start vs warm start on one problem (both to the same tolerance)."""
+    _, zero = time_to_tol(cubes, hists, None, tol)
+    t0 = time.perf_counter()
+    u0 = mlp.warm_start(cubes, hists)
+    pred_ms = 1e3 * (time.perf_counter() - t0)
+    out, warm = time_to_tol(cubes, hists, u0, tol)
+    warm.predict_ms = pred_ms
+    return zero, warm, out
