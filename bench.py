@@ -17,6 +17,8 @@ Also reported in the same JSON line:
                 on the library's stream, against MEASURED_PEAKS.json
   cpu_baseline  the CPU oracle port on a bounded sample of the same workload
   histograms    the Stage-5 pass (pyramids + binning) on the same workload
+  surface       extract_surface + compute_normals of the solved state through
+                the host-buffer C ABI call, beside the CPU oracle on a slice
   warm_start    time to relative residual 1e-4 on held-out small scenes from
                 the zero start, from the trained warm-start network
                 (tgvreconclaude_gb300/data/warmstart_nb10.npz) and from the
@@ -256,6 +258,36 @@ def measure_e2e(args, w, ctx, prm, mode, leaves, out_t, stream):
             "d2h_bytes_per_step": int(52 * n), "steps": steps, "wall_s": t_wall, "matches_device_run": same}
 
 
+def surface_eval(args, w, out_t):
+    """Surface extraction (extract_surface with has_data and normals) of the
+    solved state through the host-buffer C ABI call, and the CPU oracle on a
+    bounded contiguous Morton slice of the same input."""
+    from tgvreconclaude_gb300 import api, formats as F
+    n = len(w.cubes)
+    state = out_t.cpu().numpy().view(F.STATE_DTYPE).reshape(n).copy()
+    has = (w.hists.sum(1) > 0).astype(np.uint8)
+    o, r = np.float32(w.cfg["origin"]), float(w.cfg["r_root"])
+    api.extract_surface(w.cubes[:1000], state[:1000], o, r, has_data=has[:1000], normals=True)  # warm-up
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        v, f, _ = api.extract_surface(w.cubes, state, o, r, has_data=has, normals=True)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.median(ts))
+    res = {"cubes": n, "vertices": int(len(v)), "triangles": int(len(f)), "ms_e2e": 1e3 * t,
+           "cubes_per_s_e2e": n / t, "what": "extract_surface + compute_normals, host arrays in and out"}
+    if not args.skip_cpu:
+        sys.path.insert(0, os.path.join(HERE, "oracle"))
+        import oracle as O
+        m = min(n, args.cpu_sample)
+        t0 = time.perf_counter()
+        O.extract_surface(w.cubes[:m], state[:m], o, r, has_data=has[:m], normals=True)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": m / dt, "unit": "cubes/s", "cores": 1, "kind": "port",
+                               "sample": f"first {m} Morton-ordered cubes of the solved {args.workload} state"}
+    return res
+
+
 def warm_start_eval(args):
     """Time to relative residual 1e-4 (at most 6000 iterations per level) on
     held-out small scenes: zero start, trained network, reference initialisation."""
@@ -314,8 +346,8 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     # warm-up: the first step autotunes every level's schedule (direct launches);
-    # with per-launch timing on, the next one captures the level loop into a
-    # CUDA graph that the timed steps relaunch
+    # with per-launch timing on, the third captures the level loop into a CUDA
+    # graph (the second solve of the same problem does) that the timed steps relaunch
     for k in range(args.warmup):
         ctx.lib.tgvg_set_timing(ctx.h, int(k > 0))
         api.tgv_solve_device(cubes_t, hists_t, out_t, leaves, mode, prm)
@@ -386,6 +418,7 @@ def run_ours(args):
                   "sample": f"{len(cubes_s)} contiguous Morton-ordered cubes of {args.workload}, {args.cpu_iters} iterations per "
                             f"level, in-memory semantics, single thread"}
 
+        surf = {} if args.skip_surface else surface_eval(args, w, out_t)
         ws_eval = {} if args.skip_warm else warm_start_eval(args)
 
         depth_hist = np.bincount(w.cubes["depth"], minlength=22)
@@ -400,7 +433,8 @@ def run_ours(args):
                        "chunks": len(w.leaves), "levels": {int(k): int(v) for k, v in enumerate(depth_hist) if v},
                        "l2": "inputs larger than L2 (about 100 B of state per cube)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "histograms": hs, "warm_start": ws_eval,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "histograms": hs, "surface": surf,
+            "warm_start": ws_eval,
             "clocks": clk, "graph": last_st["graph"],
             "gpu_launches": int(launches), "leaf_iters_per_step": int(li_all / args.steps),
             "levels_detail": [{"depth": d, "active": int(a), "ms": round(m, 3), "schedule": s}
@@ -419,7 +453,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="three64")
     ap.add_argument("--seed", type=int, default=0)
@@ -432,6 +466,7 @@ def main():
     ap.add_argument("--skip-hist", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-warm", action="store_true")
+    ap.add_argument("--skip-surface", action="store_true")
     ap.add_argument("--warm-seeds", type=int, default=6)
     ap.add_argument("--max-cubes", type=int, default=0, help="truncate the workload (profiling runs)")
     ap.add_argument("--cache", default="", help="load the workload from / save it to this .npz (profiling runs)")

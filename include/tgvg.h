@@ -153,17 +153,22 @@ int tgvg_set_timing(tgvg_ctx* ctx, int on);
  * (cls = -1: every class), for one mode: 0 = two launches per iteration, 1..6 =
  * one cooperative launch per level with about 256 << k cubes per block, 7 = as 0
  * with the sweep kernels capped at 32 registers, 8 / 9 = as 0 / 7 with an L2
- * prefetch of each warp's next group, -1 = let the online autotuner choose
- * (default).  Results do not depend on it. */
+ * prefetch of each warp's next group, 10 / 11 = one launch of one thread-block
+ * cluster of 8 / 16 CTAs running every iteration (units of at most 131072
+ * cubes), 12 / 13 = as 0 / 8 with the dual sweep run from the chunk's end and
+ * the primal from its start, -1 = let the online autotuner choose (default).
+ * Results do not depend on it. */
 int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
 /* CUDA graphs for the level loop (1 = on, the default; 0 = off).  When every
  * level's schedule is already fixed (chosen by the autotuner in an earlier
  * call, set with tgvg_set_schedule, or the default of a tolerance-stopped
  * solve) and per-launch timing is off, the whole level loop -- parent init,
  * snapshots, the iteration launches and the stopping tests of every level --
- * is captured into one CUDA graph, kept in the context and relaunched by the
- * next solve of a problem with the same level sizes, leaves, parameters and
- * buffers.  Results do not depend on it. */
+ * is captured into one CUDA graph, kept in the context and relaunched by
+ * later solves of a problem with the same level sizes, leaves, parameters and
+ * buffers.  Capture happens on the second consecutive solve of such a problem
+ * (graph = 1), so one-shot solves run with direct launches (graph = 0).
+ * Results do not depend on it. */
 int tgvg_set_graphs(tgvg_ctx* ctx, int on);
 
 /* ---- Stage 5: depth maps -> histograms ------------------------------------ */
@@ -293,6 +298,41 @@ int tgvg_mlp_grad(tgvg_ctx* ctx, tgvg_mlp* m, const uint16_t* X, const float* t,
 /* Adam training over shuffled mini-batches; last_loss = mean loss of the last epoch. */
 int tgvg_mlp_train(tgvg_ctx* ctx, tgvg_mlp* m, const uint16_t* X, const float* t, int64_t n, int32_t epochs,
                    int32_t batch, float lr, uint64_t seed, float* last_loss);
+
+/* ---- surface extraction (reference src/marching_cubes.hpp) -----------------
+ * The u = 0 iso-surface of a TGV state as an indexed quad mesh, two triangles
+ * per quad, vertices merged by the reference's 60-bit quantised position.
+ * Vertices, indices and normals are bit-identical to the reference's. */
+typedef struct tgvg_mesh tgvg_mesh;
+/* extract_surface (marching_cubes.hpp:28-33, marching_cubes.cpp:63-181), with
+ * compute_normals (:185-205) when normals != 0.  has_data may be null (no
+ * filter); else one byte per cube, nonzero = has votes.  Host arrays in; the
+ * mesh is returned as a handle. */
+int tgvg_extract_surface(tgvg_ctx* ctx, const tgvg_cube* cubes, const tgvg_state* state, int64_t n,
+                         const uint8_t* has_data, const float* origin3, float r_root, int32_t normals,
+                         tgvg_mesh** out);
+/* The semantics of extract_surface_streaming (marching_cubes.cpp:374-580) over
+ * arrays: leaves in the caller's (treetop) order, Morton-sorted cubes, votes
+ * from the histograms (nbins 8 or 10); vertices are the dequantised keys. */
+int tgvg_extract_surface_leaves(tgvg_ctx* ctx, const tgvg_cube* cubes, const tgvg_state* state,
+                                const uint32_t* hists, int32_t nbins, int64_t n, const tgvg_leaf* leaves,
+                                int32_t nleaf, const float* origin3, float r_root, tgvg_mesh** out);
+/* extract_surface_streaming (marching_cubes.hpp:44-51): TGV1 cube, TGVS state,
+ * TGVT treetop and TGVH histogram files in, Wavefront file out. */
+int tgvg_extract_surface_streaming(tgvg_ctx* ctx, const char* balanced_cube_path, const char* tgv_state_path,
+                                   const char* treetop_path, const char* hist_path, const float* origin3,
+                                   float r_root, const char* out_obj_path);
+int tgvg_mesh_size(const tgvg_mesh* m, int64_t* n_verts, int64_t* n_tris, int32_t* has_normals);
+/* Copy out 3 floats per vertex, 3 indices per triangle, 3 floats per normal
+ * (any pointer may be null). */
+int tgvg_mesh_read(const tgvg_mesh* m, float* verts, uint32_t* faces, float* normals);
+void tgvg_mesh_free(tgvg_mesh* m);
+/* compute_normals (marching_cubes.hpp:55) over host arrays. */
+int tgvg_compute_normals(tgvg_ctx* ctx, const float* verts, int64_t n_verts, const uint32_t* faces,
+                         int64_t n_tris, float* normals);
+/* write_obj (marching_cubes.hpp:58): `v`, `vn` when normals is non-null, `f`. */
+int tgvg_write_obj(const char* path, const float* verts, int64_t n_verts, const uint32_t* faces, int64_t n_tris,
+                   const float* normals);
 
 /* ---- state / histogram files (reference tgv.cpp:24-46, histogram.cpp:175-218) */
 int tgvg_save_tgv(const char* path, const tgvg_state* state, int64_t n);

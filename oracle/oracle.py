@@ -365,3 +365,86 @@ __all__ = ["build", "lib", "ref", "ref_available", "compute_histograms", "pyrami
            "pyramid_dims", "project", "median_indicator", "mean_indicator", "tgv_solve",
            "ref_mipmap", "ref_compute_histograms", "ref_project", "ref_median_indicator",
            "ref_mean_indicator", "ref_tgv", "ref_pipeline_cubes", "cube_keys"]
+
+
+# ------------------------------------------------------- surface extraction ---
+
+def _mesh_out(L, h, nv, nf, normals, prefix):
+    if not h:
+        raise RuntimeError(f"{prefix}extract_surface failed")
+    v = np.zeros((nv, 3), np.float32)
+    f = np.zeros((nf, 3), np.uint32)
+    nr = np.zeros((nv, 3), np.float32) if normals else None
+    getattr(L, prefix + "mesh_read")(C.c_void_p(h), _ptr(v), _ptr(f), _ptr(nr))
+    getattr(L, prefix + "mesh_free")(C.c_void_p(h))
+    return v, f, nr
+
+
+def _surface_args(cubes, state, has_data):
+    cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    state = np.ascontiguousarray(state, STATE_DTYPE)
+    hd = None if has_data is None else np.ascontiguousarray(has_data, np.uint8)
+    return cubes, state, hd
+
+
+def extract_surface(cubes, state, origin, r_root, has_data=None, normals=False):
+    """Oracle extract_surface (+ compute_normals): (verts (nv,3), faces (nf,3), normals or None)."""
+    cubes, state, hd = _surface_args(cubes, state, has_data)
+    L = lib()
+    L.orc_extract_surface.restype = C.c_void_p
+    o = np.ascontiguousarray(origin, np.float32)
+    nv, nf = C.c_int64(), C.c_int64()
+    h = L.orc_extract_surface(_ptr(cubes), _ptr(state), C.c_int64(len(cubes)), _ptr(hd), _ptr(o),
+                              C.c_float(r_root), int(normals), C.byref(nv), C.byref(nf))
+    return _mesh_out(L, h, nv.value, nf.value, normals, "orc_")
+
+
+def extract_surface_streaming(cubes, state, hists, leaves, origin, r_root):
+    """Oracle extract_surface_streaming held in memory: (verts (nv,3) dequantised, faces (nf,3))."""
+    cubes, state, _ = _surface_args(cubes, state, None)
+    tot = np.ascontiguousarray(np.asarray(hists, np.uint32).sum(1, dtype=np.uint32))
+    lv = np.ascontiguousarray(leaves, LEAF_DTYPE)
+    L = lib()
+    L.orc_extract_surface_streaming.restype = C.c_void_p
+    o = np.ascontiguousarray(origin, np.float32)
+    nv, nf = C.c_int64(), C.c_int64()
+    h = L.orc_extract_surface_streaming(_ptr(cubes), _ptr(state), _ptr(tot), C.c_int64(len(cubes)), _ptr(lv),
+                                        len(lv), _ptr(o), C.c_float(r_root), C.byref(nv), C.byref(nf))
+    v, f, _ = _mesh_out(L, h, nv.value, nf.value, False, "orc_")
+    return v, f
+
+
+def ref_extract_surface(cubes, state, origin, r_root, has_data=None, normals=False):
+    """The reference's extract_surface (+ compute_normals) through libref."""
+    cubes, state, hd = _surface_args(cubes, state, has_data)
+    R = ref()
+    R.ref_extract_surface.restype = C.c_void_p
+    nv, nf = C.c_int64(), C.c_int64()
+    h = R.ref_extract_surface(_ptr(cubes), _ptr(state), C.c_int64(len(cubes)), _ptr(hd),
+                              C.c_float(origin[0]), C.c_float(origin[1]), C.c_float(origin[2]),
+                              C.c_float(r_root), int(normals), C.byref(nv), C.byref(nf))
+    return _mesh_out(R, h, nv.value, nf.value, normals, "ref_")
+
+
+def ref_extract_surface_streaming(cube_path, state_path, treetop_path, hist_path, origin, r_root, out_obj):
+    """The reference's extract_surface_streaming (files in, .obj out)."""
+    rc = ref().ref_extract_surface_streaming(str(cube_path).encode(), str(state_path).encode(),
+                                              str(treetop_path).encode(), str(hist_path).encode(),
+                                              C.c_float(origin[0]), C.c_float(origin[1]), C.c_float(origin[2]),
+                                              C.c_float(r_root), str(out_obj).encode())
+    assert rc == 0, rc
+
+
+def obj_text(verts, faces, normals=None):
+    """Wavefront text as the reference writes it (write_obj / the streaming
+    aggregator: `v x y z` with the stream's default 6-digit %g formatting,
+    `vn` lines and `f a//a b//b c//c` when there are normals, else 1-based
+    `f a b c`)."""
+    out = ["v %g %g %g\n" % (float(x), float(y), float(z)) for x, y, z in np.asarray(verts, np.float32)]
+    if normals is not None:
+        out += ["vn %g %g %g\n" % (float(x), float(y), float(z)) for x, y, z in np.asarray(normals, np.float32)]
+        out += ["f %d//%d %d//%d %d//%d\n" % (a + 1, a + 1, b + 1, b + 1, c + 1, c + 1)
+                for a, b, c in np.asarray(faces, np.int64)]
+    else:
+        out += ["f %d %d %d\n" % (a + 1, b + 1, c + 1) for a, b, c in np.asarray(faces, np.int64)]
+    return "".join(out)

@@ -13,6 +13,7 @@
 #include "balance.hpp"
 #include "octree_builder.hpp"
 #include "merge.hpp"
+#include "marching_cubes.hpp"
 
 #include <cstdint>
 #include <cstring>
@@ -231,6 +232,67 @@ int ref_balance_octree(const char* in_path, const char* out_path) {
 int ref_build_treetop(const char* in_path, const char* out_path) {
     try {
         build_treetop(in_path, out_path);
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// extract_surface (+ compute_normals) over caller arrays.  The mesh is kept in
+// a heap object; ref_mesh_read copies it out and ref_mesh_free releases it.
+struct RefMesh {
+    Mesh m;
+};
+
+void* ref_extract_surface(const OctreeCube* cubes, const TGVCube* state, int64_t n, const uint8_t* has_data,
+                          float ox, float oy, float oz, float r_root, int32_t normals, int64_t* nv,
+                          int64_t* nf) {
+    try {
+        std::vector<OctreeCube> cv(cubes, cubes + n);
+        std::vector<TGVCube> sv(state, state + n);
+        std::vector<bool> hd;
+        if (has_data) {
+            hd.resize(static_cast<size_t>(n));
+            for (int64_t i = 0; i < n; ++i) hd[i] = has_data[i] != 0;
+        }
+        auto* r = new RefMesh;
+        r->m = extract_surface(cv, sv, Vec3f(ox, oy, oz), r_root, hd);
+        if (normals) compute_normals(r->m);
+        *nv = static_cast<int64_t>(r->m.verts.size());
+        *nf = static_cast<int64_t>(r->m.tri_count());
+        return r;
+    } catch (const std::exception&) {
+        return nullptr;
+    }
+}
+
+void ref_mesh_read(void* h, float* verts, uint32_t* faces, float* normals) {
+    const Mesh& m = static_cast<RefMesh*>(h)->m;
+    for (size_t i = 0; i < m.verts.size(); ++i)
+        for (int k = 0; k < 3; ++k) verts[3 * i + k] = m.verts[i][k];
+    std::memcpy(faces, m.faces.data(), m.faces.size() * sizeof(uint32_t));
+    if (normals)
+        for (size_t i = 0; i < m.normals.size(); ++i)
+            for (int k = 0; k < 3; ++k) normals[3 * i + k] = m.normals[i][k];
+}
+
+int ref_mesh_write_obj(void* h, const char* path) {
+    try {
+        write_obj(path, static_cast<RefMesh*>(h)->m);
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+void ref_mesh_free(void* h) { delete static_cast<RefMesh*>(h); }
+
+int ref_extract_surface_streaming(const char* cube_path, const char* state_path, const char* treetop_path,
+                                  const char* hist_path, float ox, float oy, float oz, float r_root,
+                                  const char* out_obj) {
+    try {
+        extract_surface_streaming(cube_path, state_path, treetop_path, hist_path, Vec3f(ox, oy, oz), r_root,
+                                  out_obj);
         return 0;
     } catch (const std::exception&) {
         return -1;

@@ -677,6 +677,212 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
     return 0;
 }
 
+// ---- surface extraction (reference src/marching_cubes.cpp) ------------------
+// A quad at the zero crossing of u is placed on every face pair of cubes whose
+// u changes sign; vertices are merged by a 60-bit quantised key.
+struct SurfMesh {
+    std::vector<float> v;         // 3 per vertex
+    std::vector<uint32_t> f;      // 3 per triangle
+    std::vector<float> nrm;       // 3 per vertex (optional)
+};
+
+// World lower corner of a cube (cube_corner, marching_cubes.cpp:21-30).
+static inline void cube_corner(const Cube& c, const float* o, float r_root, float* out, float& cs) {
+    uint32_t fx, fy, fz;
+    decode(key_of(c.hi, c.lo), fx, fy, fz);
+    const int sh = 21 - c.depth;
+    cs = 2.0f * r_root / static_cast<float>(1u << c.depth);
+    out[0] = o[0] + static_cast<float>(fx >> sh) * cs;
+    out[1] = o[1] + static_cast<float>(fy >> sh) * cs;
+    out[2] = o[2] + static_cast<float>(fz >> sh) * cs;
+}
+
+// 20-bit quantisation and the packed 60-bit vertex key (marching_cubes.cpp:34-47).
+static inline uint64_t vertex_key(const float* p, const float* o, float inv) {
+    uint64_t k = 0;
+    for (int a = 0; a < 3; ++a) {
+        int q = trunc_i32((p[a] - o[a]) * inv + 0.5f);
+        if (q < 0) q = 0;
+        if (q > (1 << 20) - 1) q = (1 << 20) - 1;
+        k |= static_cast<uint64_t>(q) << (20 * a);
+    }
+    return k;
+}
+
+// The quad of face pair (i, j) seen from cube i across face f: corners v0..v3
+// (marching_cubes.cpp:124-158) and the winding flag (:167-168).
+static inline bool face_quad(const Cube& ci, const Cube& cj, float ui, float uj, int f, const float* o,
+                             float r_root, float q[4][3]) {
+    float pi[3], pj[3], cs_i, cs_j;
+    cube_corner(ci, o, r_root, pi, cs_i);
+    cube_corner(cj, o, r_root, pj, cs_j);
+    const float cs_min = cs_i < cs_j ? cs_i : cs_j;
+    const float h = cs_min * 0.5f;
+    const float t = ui / (ui - uj);
+    const int ax = f / 2;
+    float surf[3];
+    const float ci_c = pi[ax] + cs_i * 0.5f, cj_c = pj[ax] + cs_j * 0.5f;
+    surf[ax] = ci_c + t * (cj_c - ci_c);
+    const float* small = cs_i <= cs_j ? pi : pj;
+    for (int b = 0; b < 3; ++b)
+        if (b != ax) surf[b] = small[b] + h;
+    // tangential half-extents: x normal -> (y, z); y -> (z, x); z -> (x, y)
+    const int t1 = ax == 0 ? 1 : ax == 1 ? 2 : 0;
+    const int t2 = ax == 0 ? 2 : ax == 1 ? 0 : 1;
+    float a1[3] = {0.0f, 0.0f, 0.0f}, a2[3] = {0.0f, 0.0f, 0.0f};
+    a1[t1] = h;
+    a2[t2] = h;
+    for (int b = 0; b < 3; ++b) {
+        q[0][b] = (surf[b] - a1[b]) - a2[b];
+        q[1][b] = (surf[b] + a1[b]) - a2[b];
+        q[2][b] = (surf[b] + a1[b]) + a2[b];
+        q[3][b] = (surf[b] - a1[b]) + a2[b];
+    }
+    return (f % 2 == 0) ? (ui > 0.0f) : (ui < 0.0f);
+}
+
+static inline void push_quad(std::vector<uint32_t>& f, const uint32_t id[4], bool flip) {
+    if (!flip) {
+        f.insert(f.end(), {id[0], id[1], id[2], id[0], id[2], id[3]});
+    } else {
+        f.insert(f.end(), {id[0], id[2], id[1], id[0], id[3], id[2]});
+    }
+}
+
+// extract_surface (marching_cubes.cpp:63-181): neighbour by code (largest
+// index), else the parent code; self links skipped; each unordered index pair
+// judged once, by its first visitor in (cube, face) order.
+static void extract_surface(const Cube* cubes, const State* st, int64_t n, const uint8_t* has_data,
+                            const float* o, float r_root, SurfMesh& m) {
+    const float inv = static_cast<float>(1u << 20) / (2.0f * r_root);
+    std::unordered_map<uint64_t, uint32_t> cmap;
+    cmap.reserve(size_t(n) * 2);
+    for (int64_t i = 0; i < n; ++i) cmap[key_of(cubes[i].hi, cubes[i].lo)] = uint32_t(i);
+    auto find = [&](uint64_t k) -> int64_t {
+        auto it = cmap.find(k);
+        return it == cmap.end() ? -1 : int64_t(it->second);
+    };
+    std::unordered_map<uint64_t, char> seen;
+    std::unordered_map<uint64_t, uint32_t> vmap;
+    for (int64_t i = 0; i < n; ++i) {
+        const uint64_t ki = key_of(cubes[i].hi, cubes[i].lo);
+        for (int f = 0; f < 6; ++f) {
+            const uint64_t nk = face_key(ki, f, cubes[i].depth);
+            if (is_none(nk)) continue;
+            int64_t j = find(nk);
+            if (j < 0 && cubes[i].depth > 0) j = find(parent_key(nk, cubes[i].depth));
+            if (j < 0 || j == i) continue;
+            const uint64_t lo = uint64_t(std::min<int64_t>(i, j)), hi = uint64_t(std::max<int64_t>(i, j));
+            if (!seen.emplace((lo << 32) | hi, 1).second) continue;
+            if (has_data && !(has_data[i] && has_data[j])) continue;
+            const float ui = st[i].u, uj = st[j].u;
+            if ((ui >= 0.0f) == (uj >= 0.0f)) continue;
+            float q[4][3];
+            const bool flip = face_quad(cubes[i], cubes[j], ui, uj, f, o, r_root, q);
+            uint32_t id[4];
+            for (int c = 0; c < 4; ++c) {
+                auto r = vmap.emplace(vertex_key(q[c], o, inv), uint32_t(m.v.size() / 3));
+                if (r.second) m.v.insert(m.v.end(), {q[c][0], q[c][1], q[c][2]});
+                id[c] = r.first->second;
+            }
+            push_quad(m.f, id, flip);
+        }
+    }
+}
+
+// compute_normals (marching_cubes.cpp:185-205): face normals (b-a) x (c-a)
+// summed per vertex in triangle order, then divided by their length when it
+// exceeds 1e-12.
+static void compute_normals(SurfMesh& m) {
+    const size_t nv = m.v.size() / 3, nt = m.f.size() / 3;
+    m.nrm.assign(nv * 3, 0.0f);
+    for (size_t t = 0; t < nt; ++t) {
+        const float* a = &m.v[3 * m.f[3 * t]];
+        const float* b = &m.v[3 * m.f[3 * t + 1]];
+        const float* c = &m.v[3 * m.f[3 * t + 2]];
+        const float d0 = b[0] - a[0], d1 = b[1] - a[1], d2 = b[2] - a[2];
+        const float e0 = c[0] - a[0], e1 = c[1] - a[1], e2 = c[2] - a[2];
+        const float nn[3] = {d1 * e2 - d2 * e1, d2 * e0 - d0 * e2, d0 * e1 - d1 * e0};
+        for (int k = 0; k < 3; ++k)
+            for (int ax = 0; ax < 3; ++ax) m.nrm[3 * m.f[3 * t + k] + ax] += nn[ax];
+    }
+    for (size_t vtx = 0; vtx < nv; ++vtx) {
+        float* x = &m.nrm[3 * vtx];
+        const float len = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        if (len > 1e-12f) { x[0] /= len; x[1] /= len; x[2] /= len; }
+    }
+}
+
+// extract_surface_streaming (marching_cubes.cpp:374-580), held in memory:
+// leaves in the given order; neighbour candidates in the order in-leaf exact,
+// file bisection exact, in-leaf parent, file bisection parent, a candidate equal
+// to the cube itself skipped; the finer side (equal depth: smaller index) owns
+// a pair; both cubes need votes.  Vertices are numbered by first appearance and
+// placed at their dequantised keys.
+static void extract_surface_streaming(const Cube* cubes, const State* st, const uint32_t* tot, int64_t n,
+                                      const Leaf* leaves, int nleaf, const float* o, float r_root,
+                                      SurfMesh& m) {
+    const float inv = static_cast<float>(1u << 20) / (2.0f * r_root);
+    const float scale = 1.0f / inv;
+    std::vector<uint64_t> keys(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) keys[i] = key_of(cubes[i].hi, cubes[i].lo);
+    std::unordered_map<uint64_t, uint32_t> vmap;
+    std::vector<uint64_t> vkeys;
+    for (int l = 0; l < nleaf; ++l) {
+        const uint32_t a = leaves[l].first_idx, b = leaves[l].last_idx;
+        if (int64_t(a) >= n || a > b) continue;  // load_cubes_range clamps (octree_builder.cpp:131-135)
+        const uint32_t e = uint32_t(std::min<int64_t>(int64_t(b), n - 1));
+        std::unordered_map<uint64_t, uint32_t> lmap;
+        for (uint32_t g = a; g <= e; ++g) lmap[keys[g]] = g;
+        for (uint32_t gi = a; gi <= e; ++gi) {
+            const Cube& ci = cubes[gi];
+            for (int f = 0; f < 6; ++f) {
+                const uint64_t nk = face_key(keys[gi], f, ci.depth);
+                if (is_none(nk)) continue;
+                uint32_t gj = 0xffffffffu;
+                auto in_leaf = [&](uint64_t k) {
+                    if (gj != 0xffffffffu) return;
+                    auto it = lmap.find(k);
+                    if (it != lmap.end() && it->second != gi) gj = it->second;
+                };
+                auto in_file = [&](uint64_t k) {
+                    if (gj != 0xffffffffu) return;
+                    const uint32_t g = file_lookup(keys, k);
+                    if (g != 0xffffffffu && g != gi) gj = g;
+                };
+                in_leaf(nk);
+                in_file(nk);
+                if (ci.depth > 0) {
+                    const uint64_t pk = parent_key(nk, ci.depth);
+                    in_leaf(pk);
+                    in_file(pk);
+                }
+                if (gj == 0xffffffffu) continue;
+                const Cube& cj = cubes[gj];
+                if (cj.depth > ci.depth) continue;
+                if (cj.depth == ci.depth && gi > gj) continue;
+                if (tot[gi] == 0 || tot[gj] == 0) continue;
+                const float ui = st[gi].u, uj = st[gj].u;
+                if ((ui >= 0.0f) == (uj >= 0.0f)) continue;
+                float q[4][3];
+                const bool flip = face_quad(ci, cj, ui, uj, f, o, r_root, q);
+                uint32_t id[4];
+                for (int c = 0; c < 4; ++c) {
+                    const uint64_t k = vertex_key(q[c], o, inv);
+                    auto r = vmap.emplace(k, uint32_t(vkeys.size()));
+                    if (r.second) vkeys.push_back(k);
+                    id[c] = r.first->second;
+                }
+                push_quad(m.f, id, flip);
+            }
+        }
+    }
+    m.v.resize(vkeys.size() * 3);
+    for (size_t k = 0; k < vkeys.size(); ++k)
+        for (int a = 0; a < 3; ++a)
+            m.v[3 * k + a] = o[a] + static_cast<float>((vkeys[k] >> (20 * a)) & 0xFFFFFull) * scale;
+}
+
 }  // namespace orc
 
 // ============================ C API (ctypes) =================================
@@ -842,4 +1048,36 @@ int orc_stream_level(const orc::Cube* cubes, const uint32_t* hists, int64_t n, i
     std::memcpy(state, s.data(), sizeof(orc::State) * size_t(n));
     return rc;
 }
+}
+
+// ---- surface extraction entry points ----------------------------------------
+extern "C" {
+void* orc_extract_surface(const orc::Cube* cubes, const orc::State* state, int64_t n, const uint8_t* has_data,
+                          const float* origin, float r_root, int32_t normals, int64_t* nv, int64_t* nf) {
+    auto* m = new orc::SurfMesh;
+    orc::extract_surface(cubes, state, n, has_data, origin, r_root, *m);
+    if (normals) orc::compute_normals(*m);
+    *nv = int64_t(m->v.size() / 3);
+    *nf = int64_t(m->f.size() / 3);
+    return m;
+}
+
+void* orc_extract_surface_streaming(const orc::Cube* cubes, const orc::State* state, const uint32_t* hist_total,
+                                    int64_t n, const orc::Leaf* leaves, int32_t nleaf, const float* origin,
+                                    float r_root, int64_t* nv, int64_t* nf) {
+    auto* m = new orc::SurfMesh;
+    orc::extract_surface_streaming(cubes, state, hist_total, n, leaves, nleaf, origin, r_root, *m);
+    *nv = int64_t(m->v.size() / 3);
+    *nf = int64_t(m->f.size() / 3);
+    return m;
+}
+
+void orc_mesh_read(void* h, float* verts, uint32_t* faces, float* normals) {
+    const auto* m = static_cast<const orc::SurfMesh*>(h);
+    std::memcpy(verts, m->v.data(), m->v.size() * sizeof(float));
+    std::memcpy(faces, m->f.data(), m->f.size() * sizeof(uint32_t));
+    if (normals && !m->nrm.empty()) std::memcpy(normals, m->nrm.data(), m->nrm.size() * sizeof(float));
+}
+
+void orc_mesh_free(void* h) { delete static_cast<orc::SurfMesh*>(h); }
 }

@@ -1,13 +1,14 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Runs the reference's own src/histogram.cpp and src/tgv.cpp (compiled unmodified
+Runs the reference's own src/histogram.cpp, src/tgv.cpp and src/marching_cubes.cpp (compiled unmodified
 into oracle/_ref/libref.so by oracle/Makefile, with the project-written
 Eigen/TBB shims) on seeded synthetic inputs and stores inputs + outputs as
 compressed .npz files.  Needs the reference checkout (TGV_REFERENCE_DIR,
 default /root/reference); the fixtures it writes are committed so the tests can
 run where the reference is absent.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # histogram and TGV fixtures, then
+    python tests/golden/make_golden.py --mesh     # the surface fixtures (read tgv_balanced.npz)
 """
 from __future__ import annotations
 
@@ -62,7 +63,45 @@ def tgv_case(name, cubes, hists, leaves, alpha0, alpha1, iters, r_root=1.0):
     print(f"tgv_{name}: {len(cubes)} cubes, depths {np.nonzero(d)[0].tolist()}, leaves {len(leaves)}")
 
 
+def mesh_case(name, cubes, state, hists, leaves, origin, r_root):
+    """The reference's extract_surface (has_data = any vote, with normals) and
+    extract_surface_streaming (its .obj text) on one octree and state."""
+    import tempfile
+    has = (hists.sum(1) > 0).astype(np.uint8)
+    v, f, nrm = O.ref_extract_surface(cubes, state, origin, r_root, has_data=has, normals=True)
+    with tempfile.TemporaryDirectory() as td:
+        paths = [os.path.join(td, x) for x in ("c.bin", "s.bin", "t.bin", "h.bin", "m.obj")]
+        F.save_cubes(paths[0], cubes, r_root)
+        F.save_state(paths[1], state)
+        F.save_treetop(paths[2], leaves, r_root)
+        F.save_histograms(paths[3], hists)
+        O.ref_extract_surface_streaming(*paths[:4], origin, r_root, paths[4])
+        obj = open(paths[4]).read()
+    np.savez_compressed(os.path.join(HERE, f"mesh_{name}.npz"), cubes=cubes, state=state, hists=hists,
+                        leaves=leaves, origin=np.float32(origin), r_root=np.float32(r_root), has_data=has,
+                        verts=v, faces=f, normals=nrm, s_obj=np.array(obj))
+    print(f"mesh_{name}: {len(cubes)} cubes, {len(v)} vertices, {len(f)} triangles, "
+          f"streaming obj {obj.count(chr(10))} lines")
+
+
+def mesh_cases():
+    """Surface-extraction fixtures: the balanced reference octree with the
+    reference's TGV state, and a random octree with random u."""
+    O.build(ref=True)
+    g = dict(np.load(os.path.join(HERE, "tgv_balanced.npz")))
+    mesh_case("balanced", g["cubes"], g["inmem"], g["hists"], g["leaves"], (-1.5, -1.5, -1.5), 1.5)
+    rng = np.random.default_rng(7)
+    c = S.random_octree(rng, dmin=2, dmax=6, target=3000, shape="sphere", r_root=2.0)
+    st = np.zeros(len(c), F.STATE_DTYPE)
+    st["u"] = rng.uniform(-1, 1, len(c)).astype(np.float32)
+    h = S.random_histograms(rng, len(c), empty_frac=0.15)
+    lv = S.split_leaves(len(c), 4, rng, c, aligned=True)
+    mesh_case("rand", c, st, h, lv, (-2.0, -1.5, -1.0), 2.0)
+
+
 def main():
+    if "--mesh" in sys.argv:
+        return mesh_cases()
     O.build(ref=True)
     rng = np.random.default_rng(20261203)
 
@@ -98,6 +137,7 @@ def main():
     hb = O.ref_compute_histograms(cb, maps_b, (-1.5, -1.5, -1.5), 1.5)
     lv = S.split_leaves(len(cb), 3, rng, cb, aligned=True)
     tgv_case("balanced", cb, hb, lv, 2.0, 1.0, 40, r_root=1.5)
+    mesh_cases()
 
 
 if __name__ == "__main__":

@@ -1,6 +1,8 @@
-"""The C++ drop-in (tgvreconclaude_gb300/dropin/tgv_dropin.cpp) compiles against
-the reference's own headers and links into the reference's own Stage-5/6 test
-programs in place of src/histogram.cpp and src/tgv.cpp.  Needs the reference
+"""The C++ drop-in (tgvreconclaude_gb300/dropin/tgv_dropin.cpp, surface_dropin.cpp)
+compiles against the reference's own headers and links into the reference's own
+Stage-5/6 test programs in place of src/histogram.cpp and src/tgv.cpp; the
+Stage-7 replacement of src/marching_cubes.cpp compiles against the reference's
+header (its test program also needs src/qslim.cpp, hence a full Eigen).  Needs the reference
 checkout; without a GPU the programs must stop at their first call with the
 no-device error (there is no CPU path)."""
 import os
@@ -21,7 +23,7 @@ def test_dropin_links_reference_tests():
     _native.build()
     r = subprocess.run(["make", "-s", "-C", DROPIN, f"REF_DIR={REF_DIR}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    for t in ("test_stage5_dropin", "test_stage6_dropin"):
+    for t in ("test_stage5_dropin", "test_stage6_dropin", "obj/surface_dropin.o"):
         assert os.path.exists(os.path.join(DROPIN, "_build", t))
 
 

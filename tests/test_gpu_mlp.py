@@ -78,26 +78,39 @@ def test_training_reduces_loss():
 
 
 def test_trained_network_gain():
-    """Trained on six small scenes, on held-out scenes the network's u is far
+    """The shipped network (tgvreconclaude_gb300/data/warmstart_nb10.npz,
+    trained by train_warmstart on seeds 0-99) on held-out scenes: its u is far
     closer to the converged u than the zero start (the solver's fallback) and
-    no farther than the reference's median start; the solve seeded with it,
-    judged by the same stopping test, ends on the plain solver's solution.
-    Distances are taken over the cubes whose converged |u| <= 1: on the few
-    weakly observed cubes where the reference iteration has no fixed point, u
-    drifts without bound and no start can be judged.  (The number of
-    iterations to the tolerance is printed, not asserted: on these octrees the
-    finest levels' residual falls like 1/k whatever u a level starts from.)"""
-    X, t = WS.dataset(range(6))
-    m = WS.WarmStartMLP(10, seed=0)
-    m.train(X, t, epochs=20, batch=2048, lr=2e-3, seed=0)
-    for seed in (100, 101):
+    within 5 % of the reference's median start; the solve seeded with it, judged
+    by the same stopping test, ends on the plain solver's solution.  Distances
+    are taken over the cubes whose converged |u| <= 1: on the few weakly
+    observed cubes where the reference iteration has no fixed point, u drifts
+    without bound and no start can be judged.  (The number of iterations to the
+    tolerance is printed, not asserted: on these octrees the finest levels'
+    residual falls like 1/k whatever u a level starts from.)"""
+    m = WS.WarmStartMLP.load(WS.WEIGHTS)
+    for seed in (1000, 1001):
         cubes, hists = WS.small_scene(seed, "torus" if seed % 2 == 0 else "three")
         ref, _ = WS.converged_u(cubes, hists)
         ok = np.abs(ref) <= 1.0
         assert ok.mean() > 0.99
         err = WS.start_errors(m, cubes[ok], hists[ok], ref[ok])
         assert err["network"] < 0.25 * err["zero"], err
-        assert err["network"] <= 1.02 * err["median"], err
+        assert err["network"] <= 1.05 * err["median"], err
         zero, warm, out = WS.compare(m, cubes, hists, tol=1e-4)
         print(seed, err, "leaf-iterations zero %d warm %d" % (zero.leaf_iters, warm.leaf_iters))
-        assert np.sqrt(np.mean((out["u"][ok] - ref[ok]) ** 2)) < 0.02
+        # the end points agree wherever both solves stay bounded (the unstable
+        # cubes can drift in one solve and not the other)
+        both = ok & (np.abs(out["u"]) <= 1.0)
+        assert both.mean() > 0.98, both.mean()
+        assert np.sqrt(np.mean((out["u"][both] - ref[both]) ** 2)) < 0.02
+
+
+def test_training_on_solver_pairs():
+    """Two scenes' (features, converged u - median) pairs: GPU training lowers
+    the mean squared error."""
+    X, t = WS.dataset(range(2))
+    m = WS.WarmStartMLP(10, seed=0)
+    l0, _ = m.grad(X, t)
+    l1 = m.train(X, t, epochs=10, batch=2048, lr=2e-3, seed=0)
+    assert l1 < 0.5 * l0, (l0, l1)

@@ -170,7 +170,7 @@ def test_tgv_random_vs_oracle(oracle_lib, seed):
 
 
 def test_tgv_autotuned_schedules_are_exact(oracle_lib):
-    """400 iterations: the first solve tunes each level's schedule online
+    """500 iterations: the first solve tunes each level's schedule online
     (per-sweep launches with and without register cap and L2 prefetch vs one
     cooperative launch per level, several grid sizes), the second reuses the
     tuned table; both stay bit-identical."""
@@ -179,20 +179,49 @@ def test_tgv_autotuned_schedules_are_exact(oracle_lib):
     hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.05)
     leaves = S.split_leaves(len(cubes), 5, rng, cubes, aligned=True)
     for mode in ("inmem", "stream"):
-        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, alpha0=2.0, alpha1=1.0, iters=400, nthreads=8)
+        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, alpha0=2.0, alpha1=1.0, iters=500, nthreads=8)
         for _ in range(2):
-            out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=400))
+            out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=500))
             assert_state_equal(out, ref, f"autotuned {mode}")
 
 
 @pytest.mark.parametrize("mode", ["inmem", "oc", "stream"])
+def test_tgv_every_schedule_is_exact(oracle_lib, mode):
+    """Each of the fourteen iteration schedules (per-sweep launches with and
+    without register cap / L2 prefetch / swapped sweep directions, six
+    persistent grid sizes, clusters of 8 and 16 CTAs), forced for every level,
+    with and without the stopping test, gives the oracle's state bit for bit."""
+    ctx = api.context()
+    rng = np.random.default_rng(41)
+    cubes = S.random_octree(rng, dmin=1, dmax=6, target=12000, shape="sphere")
+    hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.0)
+    leaves = S.split_leaves(len(cubes), 5, rng, cubes, aligned=True)
+    fixed, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 40, nthreads=8)
+    stop, rst = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 300, tol=1e-3, check_every=10,
+                                     nthreads=8)
+    try:
+        for cfg in range(14):
+            ctx.set_schedule(mode, -1, cfg)
+            out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=40))
+            assert set(st["schedule"]) == {cfg}
+            assert_state_equal(out, fixed, f"schedule {cfg} {mode}")
+            out, st = api.tgv_solve(cubes, hists, leaves, mode,
+                                    api.TGVParams(alpha0=2.0, alpha1=1.0, iters=300, tol=1e-3, check_every=10))
+            assert_state_equal(out, stop, f"schedule {cfg} {mode} stopping")
+            assert st["iters_run"] == [r["iters_run"] for r in rst]
+    finally:
+        ctx.set_schedule(mode, -1, -1)
+
+
+@pytest.mark.parametrize("mode", ["inmem", "oc", "stream"])
 def test_tgv_graph_capture_and_replay(oracle_lib, mode):
-    """With the schedule fixed, the whole level loop is captured into one CUDA
-    graph (graph = 1) and relaunched for the same problem (graph = 2).  A
-    tolerance-stopped solve: graphs off, captured and replayed all give the
-    oracle's state and per-level iteration counts bit for bit.  A fixed-count
-    solve after resetting the schedule table: the first call autotunes with
-    direct launches (graph = 0), the next two capture and replay."""
+    """With the schedule fixed, the second solve of a problem captures the
+    whole level loop into one CUDA graph (graph = 1) and later solves relaunch
+    it (graph = 2).  A tolerance-stopped solve: graphs off, first sighting,
+    captured and replayed all give the oracle's state and per-level iteration
+    counts bit for bit.  A fixed-count solve after resetting the schedule
+    table: the first call autotunes with direct launches (graph = 0), the next
+    is a first sighting, then capture and replay."""
     ctx = api.context()
     rng = np.random.default_rng(31)
     cubes = S.random_octree(rng, dmin=1, dmax=6, target=20000, shape="sphere")
@@ -203,23 +232,23 @@ def test_tgv_graph_capture_and_replay(oracle_lib, mode):
     prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=400, tol=1e-4, check_every=10)
     try:
         runs = []
-        for graphs in (False, True, True):
+        for graphs in (False, True, True, True):
             ctx.set_graphs(graphs)
             runs.append(api.tgv_solve(cubes, hists, leaves, mode, prm))
-        assert [st["graph"] for _, st in runs] == [0, 1, 2]
+        assert [st["graph"] for _, st in runs] == [0, 0, 1, 2]
         for out, st in runs:
             assert_state_equal(out, ref, f"graph {st['graph']} {mode}")
             assert st["iters_run"] == [r["iters_run"] for r in rst]
-        assert runs[1][1]["kernel_launches"] == runs[2][1]["kernel_launches"] > 0
+        assert runs[2][1]["kernel_launches"] == runs[3][1]["kernel_launches"] > 0
 
-        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 400, nthreads=8)
+        ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 500, nthreads=8)
         ctx.set_schedule(mode, -1, -1)
-        prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=400)
-        runs = [api.tgv_solve(cubes, hists, leaves, mode, prm) for _ in range(3)]
-        assert [st["graph"] for _, st in runs] == [0, 1, 2]
+        prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=500)
+        runs = [api.tgv_solve(cubes, hists, leaves, mode, prm) for _ in range(4)]
+        assert [st["graph"] for _, st in runs] == [0, 0, 1, 2]
         for out, st in runs:
             assert_state_equal(out, ref, f"tuned graph {st['graph']} {mode}")
-        assert runs[1][1]["schedule"] == runs[2][1]["schedule"]
+        assert runs[1][1]["schedule"] == runs[2][1]["schedule"] == runs[3][1]["schedule"]
     finally:
         ctx.set_graphs(True)
 

@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libtgvg.so")
-SOURCES = ["capi.cu", "hist.cu", "tgv.cu", "mlp.cu"]
+SOURCES = ["capi.cu", "hist.cu", "tgv.cu", "mlp.cu", "surface.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
@@ -145,6 +145,16 @@ _SIGS = {
     "tgvg_mlp_warm_start_dev": ([P, P, P, P, C.c_int64, C.c_int32, P, C.c_int32, P], C.c_int),
     "tgvg_mlp_grad": ([P, P, P, P, C.c_int64, P, P], C.c_int),
     "tgvg_mlp_train": ([P, P, P, P, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P], C.c_int),
+    "tgvg_extract_surface": ([P, P, P, C.c_int64, P, P, C.c_float, C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
+    "tgvg_extract_surface_leaves": ([P, P, P, P, C.c_int32, C.c_int64, P, C.c_int32, P, C.c_float,
+                                     C.POINTER(C.c_void_p)], C.c_int),
+    "tgvg_extract_surface_streaming": ([P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, P, C.c_float,
+                                        C.c_char_p], C.c_int),
+    "tgvg_mesh_size": ([P, P, P, P], C.c_int),
+    "tgvg_mesh_read": ([P, P, P, P], C.c_int),
+    "tgvg_mesh_free": ([P], None),
+    "tgvg_compute_normals": ([P, P, C.c_int64, P, C.c_int64, P], C.c_int),
+    "tgvg_write_obj": ([C.c_char_p, P, C.c_int64, P, C.c_int64, P], C.c_int),
     "tgvg_save_tgv": ([C.c_char_p, P, C.c_int64], C.c_int),
     "tgvg_load_tgv": ([C.c_char_p, P, C.c_int64], C.c_int64),
     "tgvg_save_histograms": ([C.c_char_p, P, C.c_int64], C.c_int),

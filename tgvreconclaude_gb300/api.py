@@ -345,3 +345,80 @@ def load_histograms_range(path, first_idx, last_idx):
     if first_idx >= len(h) or first_idx > last_idx:
         return h[:0]
     return h[first_idx:min(last_idx + 1, len(h))]
+
+
+# ------------------------------------------------------ surface extraction ---
+
+def _take_mesh(ctx, h):
+    nv, nf, hn = C.c_int64(), C.c_int64(), C.c_int32()
+    ctx.check(ctx.lib.tgvg_mesh_size(h, C.byref(nv), C.byref(nf), C.byref(hn)), "tgvg_mesh_size")
+    v = np.zeros((nv.value, 3), np.float32)
+    f = np.zeros((nf.value, 3), np.uint32)
+    nrm = np.zeros((nv.value, 3), np.float32) if hn.value else None
+    ctx.check(ctx.lib.tgvg_mesh_read(h, _p(v), _p(f), _p(nrm)), "tgvg_mesh_read")
+    ctx.lib.tgvg_mesh_free(h)
+    return v, f, nrm
+
+
+def extract_surface(cubes, state, origin, r_root, has_data=None, normals=False):
+    """extract_surface (reference src/marching_cubes.hpp:28-33) on the GPU,
+    followed by compute_normals when normals=True.  Returns (verts (nv, 3)
+    float32, faces (nf, 3) uint32, normals (nv, 3) or None)."""
+    ctx = context()
+    cubes = np.ascontiguousarray(cubes, F.CUBE_DTYPE)
+    state = np.ascontiguousarray(state, F.STATE_DTYPE)
+    hd = None if has_data is None else np.ascontiguousarray(has_data, np.uint8)
+    o = np.ascontiguousarray(origin, np.float32)
+    h = C.c_void_p()
+    ctx.check(ctx.lib.tgvg_extract_surface(ctx.h, _p(cubes), _p(state), len(cubes), _p(hd), _p(o), C.c_float(r_root),
+                                           int(bool(normals)), C.byref(h)), "tgvg_extract_surface")
+    return _take_mesh(ctx, h)
+
+
+def extract_surface_leaves(cubes, state, hists, leaves, origin, r_root):
+    """The streaming extraction's semantics (reference marching_cubes.cpp:374-580)
+    over arrays: returns (verts dequantised (nv, 3), faces (nf, 3))."""
+    ctx = context()
+    cubes = np.ascontiguousarray(cubes, F.CUBE_DTYPE)
+    state = np.ascontiguousarray(state, F.STATE_DTYPE)
+    hists = np.ascontiguousarray(hists, np.uint32)
+    lv = np.ascontiguousarray(leaves, F.LEAF_DTYPE)
+    o = np.ascontiguousarray(origin, np.float32)
+    h = C.c_void_p()
+    ctx.check(ctx.lib.tgvg_extract_surface_leaves(ctx.h, _p(cubes), _p(state), _p(hists),
+                                                  hists.shape[1] if hists.ndim == 2 else 8, len(cubes), _p(lv),
+                                                  len(lv), _p(o), C.c_float(r_root), C.byref(h)),
+              "tgvg_extract_surface_leaves")
+    v, f, _ = _take_mesh(ctx, h)
+    return v, f
+
+
+def extract_surface_streaming(balanced_cube_path, tgv_state_path, treetop_path, hist_path, origin, r_root,
+                              out_obj_path):
+    """extract_surface_streaming (reference src/marching_cubes.hpp:44-51): files in, .obj out."""
+    ctx = context()
+    o = np.ascontiguousarray(origin, np.float32)
+    ctx.check(ctx.lib.tgvg_extract_surface_streaming(ctx.h, str(balanced_cube_path).encode(),
+                                                     str(tgv_state_path).encode(), str(treetop_path).encode(),
+                                                     str(hist_path).encode(), _p(o), C.c_float(r_root),
+                                                     str(out_obj_path).encode()), "tgvg_extract_surface_streaming")
+
+
+def compute_normals(verts, faces):
+    """compute_normals (reference src/marching_cubes.hpp:55) on the GPU."""
+    ctx = context()
+    v = np.ascontiguousarray(verts, np.float32)
+    f = np.ascontiguousarray(faces, np.uint32)
+    nrm = np.zeros_like(v)
+    ctx.check(ctx.lib.tgvg_compute_normals(ctx.h, _p(v), len(v), _p(f), len(f), _p(nrm)), "tgvg_compute_normals")
+    return nrm
+
+
+def write_obj(path, verts, faces, normals=None):
+    """write_obj (reference src/marching_cubes.hpp:58)."""
+    v = np.ascontiguousarray(verts, np.float32)
+    f = np.ascontiguousarray(faces, np.uint32)
+    nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+    rc = N.lib().tgvg_write_obj(str(path).encode(), _p(v), len(v), _p(f), len(f), _p(nrm))
+    if rc:
+        raise RuntimeError(f"write_obj: {N.lib().tgvg_strerror(rc).decode()}")

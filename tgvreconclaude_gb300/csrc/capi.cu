@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fileio.h"
 
 // ------------------------------------------------------------------ ctx ---
 
@@ -77,7 +78,7 @@ extern "C" void tgvg_level_thresholds(float* t13) {
 }
 
 extern "C" int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg) {
-    if (!ctx || mode < 0 || mode > 2 || cls < -1 || cls > 31 || cfg < -1 || cfg > 9) return TGVG_ERR_INVALID;
+    if (!ctx || mode < 0 || mode > 2 || cls < -1 || cls > 31 || cfg < -1 || cfg > 13) return TGVG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     for (int c = 0; c < 32; ++c)
         if (cls < 0 || c == cls) ctx->tune[mode][c] = cfg;
@@ -166,50 +167,8 @@ extern "C" int tgvg_destroy(tgvg_ctx* ctx) {
 }
 
 // ---------------------------------------------------------------- files ---
-namespace {
+using namespace tgvg::fileio;
 
-int read_file(const char* path, std::vector<char>& out) {
-    FILE* f = path ? std::fopen(path, "rb") : nullptr;
-    if (!f) return TGVG_ERR_IO;
-    std::fseek(f, 0, SEEK_END);
-    long sz = std::ftell(f);
-    std::fseek(f, 0, SEEK_SET);
-    out.resize(sz > 0 ? size_t(sz) : 0);
-    size_t got = out.empty() ? 0 : std::fread(out.data(), 1, out.size(), f);
-    std::fclose(f);
-    return got == out.size() ? TGVG_OK : TGVG_ERR_IO;
-}
-
-int write_file(const char* path, const void* hdr, size_t nh, const void* body, size_t nb) {
-    FILE* f = path ? std::fopen(path, "wb") : nullptr;
-    if (!f) return TGVG_ERR_IO;
-    bool ok = std::fwrite(hdr, 1, nh, f) == nh;
-    if (ok && nb) ok = std::fwrite(body, 1, nb, f) == nb;
-    ok = (std::fclose(f) == 0) && ok;
-    return ok ? TGVG_OK : TGVG_ERR_IO;
-}
-
-uint32_t u32_at(const std::vector<char>& b, size_t off) {
-    uint32_t v;
-    std::memcpy(&v, b.data() + off, 4);
-    return v;
-}
-
-// TGV1 cube file (octree_builder.hpp:8-19): 16-byte header then cubes.
-int load_cube_file(const char* path, std::vector<tgvg_cube>& cubes, float* r_root) {
-    std::vector<char> b;
-    int rc = read_file(path, b);
-    if (rc) return rc;
-    if (b.size() < 16 || std::memcmp(b.data(), "TGV1", 4) != 0) return TGVG_ERR_FORMAT;
-    uint32_t n = u32_at(b, 12);
-    if (b.size() < 16 + size_t(n) * sizeof(tgvg_cube)) return TGVG_ERR_FORMAT;
-    if (r_root) std::memcpy(r_root, b.data() + 8, 4);
-    cubes.resize(n);
-    if (n) std::memcpy(cubes.data(), b.data() + 16, size_t(n) * sizeof(tgvg_cube));
-    return TGVG_OK;
-}
-
-}  // namespace
 
 extern "C" int tgvg_save_tgv(const char* path, const tgvg_state* state, int64_t n) {
     if (n < 0 || (n > 0 && !state) || n > 0xffffffffll) return TGVG_ERR_INVALID;

@@ -95,6 +95,19 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
     x ^= x >> 33;
     return x;
 }
+// Insert `key` for index i: the slot keeps the smallest and largest index.
+__device__ __forceinline__ void hash_insert(const HashView& h, uint64_t key, int i) {
+    uint64_t s = mix64(key) & h.mask;
+    for (uint64_t probe = 0; probe <= h.mask; ++probe) {
+        const unsigned long long prev = atomicCAS(h.keys + s, (unsigned long long)NO_KEY, (unsigned long long)key);
+        if (prev == (unsigned long long)NO_KEY || prev == key) {
+            if (h.rmin) atomicMin(h.rmin + s, i);
+            if (h.rmax) atomicMax(h.rmax + s, i);
+            return;
+        }
+        s = (s + 1) & h.mask;
+    }
+}
 __device__ __forceinline__ int hash_find(const HashView& h, uint64_t key) {
     uint64_t s = mix64(key) & h.mask;
     for (uint64_t probe = 0; probe <= h.mask; ++probe) {
@@ -138,6 +151,11 @@ enum BufId {
     B_Q1, B_DAT, B_SNAP, B_LID, B_LEAVES, B_ACC, B_FLAGS, B_RANGES, B_RESID, B_LVSTAT,
     // learned warm start
     B_M_X, B_M_T, B_M_IDX, B_M_Y, B_M_LEAVES, B_M_LEAFID,
+    // surface extraction
+    B_S_CUBES, B_S_STATE, B_S_KEYS, B_S_DEPTH, B_S_U, B_S_HD, B_S_HKEYS, B_S_HMIN, B_S_HMAX, B_S_NBR,
+    B_S_FLAGS, B_S_QIDX, B_S_SCAN, B_S_RANK, B_S_LEAF, B_S_QKEY, B_S_QPOS, B_S_QFLIP, B_S_VTK, B_S_VTF,
+    B_S_SLOT, B_S_VFLAG, B_S_VID, B_S_VERTS, B_S_FACES, B_S_TN, B_S_VCNT, B_S_VSTART, B_S_VCUR, B_S_VLIST,
+    B_S_NRM,
     B_COUNT
 };
 
@@ -156,10 +174,12 @@ struct tgvg_ctx {
     std::vector<cudaEvent_t> tev;      // pool for those events
     int tune[3][32];                   // chosen iteration schedule per mode and log2(size) class, -1 = untuned
     int coop_max[3][2] = {};           // co-resident blocks of the persistent kernel per mode / stop
+    int cluster_max[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};  // usable cluster size per mode / stop (-1 unknown)
     int iter_occ[3][2][2] = {};        // blocks/SM of the sweep kernels [mode][register-capped][dual, primal]
     cudaEvent_t lev_ev[2 * TGVG_MAX_LEVELS] = {};  // per-level start/end
     bool graphs = true;                // capture the level loop into a CUDA graph when possible
     std::vector<uint64_t> graph_key;   // problem signature of the cached graph
+    std::vector<uint64_t> graph_seen;  // signature of the last solve run without a graph
     cudaGraphExec_t graph_exec = nullptr;
     int64_t graph_kernels = 0;         // kernel nodes in the cached graph
     bool capturing = false;            // the level loop is being captured

@@ -158,18 +158,7 @@ __global__ void k_bucket_scatter(int n, int mode, const int* __restrict__ depth,
 
 __global__ void k_hash_insert(int n, const unsigned long long* __restrict__ keys, HashView h) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const unsigned long long key = keys[i];
-    uint64_t s = mix64(key) & h.mask;
-    for (uint64_t probe = 0; probe <= h.mask; ++probe) {
-        const unsigned long long prev = atomicCAS(h.keys + s, (unsigned long long)NO_KEY, key);
-        if (prev == (unsigned long long)NO_KEY || prev == key) {
-            atomicMin(h.rmin + s, i);
-            atomicMax(h.rmax + s, i);
-            return;
-        }
-        s = (s + 1) & h.mask;
-    }
+    if (i < n) hash_insert(h, keys[i], i);
 }
 
 // Resolve one neighbour code into a position (or -1), with the semantics of
@@ -352,6 +341,7 @@ struct IterArgs {
     int* iters_run;
     double* resid;
     int pf;               // per-launch schedules: L2 prefetch of the warp's next group (0 = off)
+    int swap;             // per-launch schedules: dual sweep in reverse order, primal forward
 };
 
 // Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
@@ -548,10 +538,11 @@ template <int MODE, bool RES, bool STOP, bool CG, bool DUAL, bool REV>
 __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpAcc& wa) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int ngroups = (end - beg + 31) >> 5;
+    const bool rev = CG ? REV : (REV != (a.swap != 0));
     for (int gi = warp; gi < ngroups; gi += nw) {
-        const int g = REV ? (ngroups - 1 - gi) : gi;
+        const int g = rev ? (ngroups - 1 - gi) : gi;
         if (!CG && a.pf > 0 && gi + a.pf * nw < ngroups) {
-            const int gn = REV ? (ngroups - 1 - (gi + a.pf * nw)) : gi + a.pf * nw;
+            const int gn = rev ? (ngroups - 1 - (gi + a.pf * nw)) : gi + a.pf * nw;
             prefetch_group<DUAL>(a, beg + gn * 32, end, lane);
         }
         const int p = beg + g * 32 + lane;
@@ -669,6 +660,41 @@ __global__ void __launch_bounds__(ITER_BLOCK) k_level_persistent(IterArgs a) {
     }
 }
 
+// Cluster-wide barrier of all threads of a thread-block cluster, with release /
+// acquire ordering at cluster scope (the hardware barrier: nothing to poll).
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Every iteration of one small level in ONE launch of a single thread-block
+// cluster (8 or 16 CTAs of 1024 threads on one GPC): as k_level_persistent,
+// with the hardware cluster barrier in place of the software grid barrier, so
+// an iteration costs two sweeps of L2-resident state plus two barriers.
+constexpr int CLUSTER_BLOCK = 1024;
+template <int MODE, bool STOP>
+__global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_cluster(IterArgs a) {
+    const int beg = a.o + blockIdx.x * a.chunk;
+    const int end = min(a.o + a.n, beg + a.chunk);
+    for (int i = 0; i < a.iters; ++i) {
+        const int it = a.it0 + i;
+        if (STOP && MODE != M_STREAM && *(volatile int*)(a.done + a.slot0)) break;
+        const bool res = STOP && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
+        WarpAcc wd, wp;
+        if (res) sweep<MODE, true, STOP, true, true, false>(a, beg, end, wd);
+        else sweep<MODE, false, STOP, true, true, false>(a, beg, end, wd);
+        if (res) wd.flush(a.acc, 1, threadIdx.x & 31);
+        cluster_barrier();
+        if (res) sweep<MODE, true, STOP, true, false, false>(a, beg, end, wp);
+        else sweep<MODE, false, STOP, true, false, false>(a, beg, end, wp);
+        if (res) {
+            wp.flush(a.acc, 0, threadIdx.x & 31);
+            cluster_barrier();
+            if (blockIdx.x == 0) check_slots<MODE>(a, it);
+        }
+        cluster_barrier();
+    }
+}
+
 // Stopping test after a residual iteration: relative fixed-point residual
 // (|x+ - x| + |y+ - y|) / (|x+| + |y+|) in FP64 per slot (sigma = tau).
 __global__ void k_check(int s0, int ns, double* __restrict__ acc, int* __restrict__ done, float tol, int iter,
@@ -746,11 +772,52 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 // changes a result, only the time.
 // cfg 7 (CFG_LEAN): as cfg 0 with the sweep kernels capped at 32 registers.
 // cfg 8 / 9: as cfg 0 / 7 with an L2 prefetch of each warp's next group.
+// cfg 10 / 11: every iteration in one launch of one thread-block cluster of
+//   8 / 16 CTAs (k_level_cluster), for small units.
+// cfg 12 / 13: as cfg 0 / 8 with the sweep directions swapped (dual sweep from
+//   the chunk's end, primal from its start), so that each sweep meets the
+//   neighbours it gathers right after visiting them.
 static constexpr int TUNE_SEG = 16;
 static constexpr int N_PERSIST_CFG = 6;
 static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
-static inline bool per_launch_cfg(int cfg) { return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF; }
+static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13;
+static inline bool per_launch_cfg(int cfg) {
+    return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP || cfg == CFG_SWAP_PF;
+}
+static constexpr int CFG_CLUSTER8 = 10, CFG_CLUSTER16 = 11;
+static constexpr int CLUSTER_MAX_N = 1 << 17;  // cluster schedules are candidates up to this unit size
+
+// Largest usable cluster size of k_level_cluster for this mode / stop variant
+// (16 when the device accepts non-portable clusters of 16 such CTAs, else 8, or
+// 0 when not even 8 fit), cached in the context.
+template <int MODE>
+static int cluster_capacity(tgvg_ctx* ctx, bool stop, int* out) {
+    int& c = ctx->cluster_max[MODE][stop ? 1 : 0];
+    if (c < 0) {
+        const void* k = stop ? (const void*)k_level_cluster<MODE, true> : (const void*)k_level_cluster<MODE, false>;
+        c = 0;
+        for (int cs : {16, 8}) {
+            if (cs == 16 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(cs);
+            cfg.blockDim = dim3(CLUSTER_BLOCK);
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int nc = 0;
+            if (cudaOccupancyMaxActiveClusters(&nc, k, &cfg) == cudaSuccess && nc > 0) { c = cs; break; }
+            cudaGetLastError();
+        }
+    }
+    *out = c;
+    return TGVG_OK;
+}
 
 static int persist_grid(int n, int cfg, int cmax) {
     const int cpb = 256 << cfg;
@@ -787,7 +854,8 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
     if (count <= 0) return TGVG_OK;
     if (per_launch_cfg(cfg)) {
         const bool lean = cfg == CFG_LEAN || cfg == CFG_LEAN_PF;
-        a.pf = (cfg == CFG_PF || cfg == CFG_LEAN_PF) ? 1 : 0;
+        a.pf = (cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP_PF) ? 1 : 0;
+        a.swap = (cfg == CFG_SWAP || cfg == CFG_SWAP_PF) ? 1 : 0;
         int rc = iter_occupancy<MODE>(ctx);
         if (rc) return rc;
         for (int it = it0; it < it0 + count; ++it) {
@@ -809,6 +877,30 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
                 TGVG_LAUNCHED(ctx);
             }
         }
+        return TGVG_OK;
+    }
+    if (cfg == CFG_CLUSTER8 || cfg == CFG_CLUSTER16) {
+        const int cs = cfg == CFG_CLUSTER16 ? 16 : 8;
+        int cmax = 0;
+        const int rc = cluster_capacity<MODE>(ctx, stop, &cmax);  // also opts the kernel in to 16-CTA clusters
+        if (rc) return rc;
+        if (cs > cmax) return ctx->fail(TGVG_ERR_INVALID, "thread-block cluster size not supported by the device");
+        a.chunk = ((a.n + cs - 1) / cs + 31) / 32 * 32;
+        a.it0 = it0;
+        a.iters = count;
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(cs);
+        lc.blockDim = dim3(CLUSTER_BLOCK);
+        lc.stream = ctx->stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        cudaError_t e = stop ? cudaLaunchKernelEx(&lc, k_level_cluster<MODE, true>, a)
+                             : cudaLaunchKernelEx(&lc, k_level_cluster<MODE, false>, a);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "cluster launch");
+        ++ctx->kernels;
         return TGVG_OK;
     }
     int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
@@ -835,7 +927,7 @@ template <int MODE>
 static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& cands) {
     int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
     if (rc) return rc;
-    cands = {0, CFG_LEAN, CFG_PF, CFG_LEAN_PF};
+    cands = {0, CFG_LEAN, CFG_PF, CFG_LEAN_PF, CFG_SWAP, CFG_SWAP_PF};
     int last_grid = -1;
     if (n <= (1 << 22))
         for (int k = 1; k <= N_PERSIST_CFG; ++k) {
@@ -843,6 +935,12 @@ static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& ca
             if (g != last_grid) cands.push_back(k);
             last_grid = g;
         }
+    if (n <= CLUSTER_MAX_N) {
+        int cs = 0;
+        if ((rc = cluster_capacity<MODE>(ctx, stop, &cs))) return rc;
+        if (cs >= 8) cands.push_back(CFG_CLUSTER8);
+        if (cs >= 16) cands.push_back(CFG_CLUSTER16);
+    }
     return TGVG_OK;
 }
 
@@ -863,7 +961,14 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
         *cfg = per_launch_cfg(tuned) ? tuned : 0;
         return TGVG_OK;
     }
-    if (tuned >= 0) { *cfg = tuned; return TGVG_OK; }
+    if (tuned >= 0) {
+        *cfg = tuned;
+        if (tuned == CFG_CLUSTER8 || tuned == CFG_CLUSTER16) {  // set up before any stream capture
+            int cs = 0;
+            return cluster_capacity<MODE>(ctx, stop, &cs);
+        }
+        return TGVG_OK;
+    }
     std::vector<int> cands;
     if ((rc = tune_candidates<MODE>(ctx, n, stop, cands))) return rc;
     if (!stop && (int)cands.size() * TUNE_SEG * 2 <= iters) { *cfg = -1; return TGVG_OK; }
@@ -1218,7 +1323,14 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
             ctx->kernels += ctx->graph_kernels;
             for (int k = 0; k < nlv; ++k) used[k] = levels[k].us.empty() ? -1 : levels[k].us.back().cfg;
             st.graph = 2;
+        } else if (key != ctx->graph_seen) {
+            // first sighting of this problem: direct launches (a one-shot solve
+            // never pays for capture and instantiation); the next one captures
+            ctx->graph_seen = std::move(key);
+            const int rc = enqueue(false);
+            if (rc) return rc;
         } else {
+            ctx->graph_seen.clear();
             if (ctx->graph_exec) {
                 cudaGraphExecDestroy(ctx->graph_exec);
                 ctx->graph_exec = nullptr;

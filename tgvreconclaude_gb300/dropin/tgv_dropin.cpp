@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "tgvg.h"
+#include "dropin_ctx.h"
 
 static_assert(sizeof(OctreeCube) == sizeof(tgvg_cube), "OctreeCube layout");
 static_assert(sizeof(TGVCube) == sizeof(tgvg_state), "TGVCube layout");
@@ -38,23 +39,8 @@ static_assert(sizeof(CubeHistogram) == 32, "CubeHistogram layout");
 
 namespace {
 
-tgvg_ctx* ctx() {
-    static std::once_flag once;
-    static tgvg_ctx* c = nullptr;
-    static int rc = 0;
-    std::call_once(once, [] { rc = tgvg_create(0, &c); });
-    if (rc != TGVG_OK) throw std::runtime_error(std::string("tgvg_create: ") + tgvg_strerror(rc));
-    return c;
-}
-
-void check(int rc, const char* what) {
-    if (rc != TGVG_OK) {
-        std::string msg = std::string(what) + ": " + tgvg_strerror(rc);
-        const char* d = tgvg_last_error(ctx());
-        if (d && *d) msg += std::string(" (") + d + ")";
-        throw std::runtime_error(msg);
-    }
-}
+tgvg_ctx* ctx() { return tgvg_dropin_ctx(); }
+void check(int rc, const char* what) { tgvg_dropin_check(rc, what); }
 
 tgvg_camera camera_of(const DepthMipmap& m) {
     tgvg_camera c{};

@@ -14,6 +14,7 @@ tolerance, so the prediction only changes how many iterations that takes.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import time
 from dataclasses import dataclass
 
@@ -146,6 +147,8 @@ def small_scene(seed: int, kind: str = "torus", device: str = "cuda"):
 
 
 SOLVE = dict(alpha0=2.0, alpha1=1.0)
+# The shipped network, trained by train_warmstart on seeds 0-99.
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "warmstart_nb10.npz")
 
 
 def converged_u(cubes, hists, tol: float = 1e-6, max_iters: int = 6000):
