@@ -342,6 +342,7 @@ struct IterArgs {
     double* resid;
     int pf;               // per-launch schedules: L2 prefetch of the warp's next group (0 = off)
     int swap;             // per-launch schedules: dual sweep in reverse order, primal forward
+    int band;             // per-launch schedules: warps stride over the whole unit (grid-stride band)
 };
 
 // Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
@@ -534,15 +535,27 @@ __device__ __forceinline__ void prefetch_group(const IterArgs& a, int q0, int en
     if (line && q0 < end) asm volatile("prefetch.global.L2 [%0];" ::"l"(line));
 }
 
+// Warp w of the block takes groups w, w + nw, ... of [beg, end); in band mode
+// (per-launch schedules with a.band) the range is the whole unit and the
+// global warp g takes groups g, g + (all warps), ..., so that all warps work
+// on one narrow band of positions that moves through the unit and a cube's
+// neighbours are read while their lines are still in L2.
 template <int MODE, bool RES, bool STOP, bool CG, bool DUAL, bool REV>
 __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpAcc& wa) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int g0 = warp, gs = blockDim.x >> 5;
+    if (!CG && a.band) {
+        beg = a.o;
+        end = a.o + a.n;
+        g0 = blockIdx.x * gs + warp;
+        gs *= gridDim.x;
+    }
     const int ngroups = (end - beg + 31) >> 5;
     const bool rev = CG ? REV : (REV != (a.swap != 0));
-    for (int gi = warp; gi < ngroups; gi += nw) {
+    for (int gi = g0; gi < ngroups; gi += gs) {
         const int g = rev ? (ngroups - 1 - gi) : gi;
-        if (!CG && a.pf > 0 && gi + a.pf * nw < ngroups) {
-            const int gn = rev ? (ngroups - 1 - (gi + a.pf * nw)) : gi + a.pf * nw;
+        if (!CG && a.pf > 0 && gi + a.pf * gs < ngroups) {
+            const int gn = rev ? (ngroups - 1 - (gi + a.pf * gs)) : gi + a.pf * gs;
             prefetch_group<DUAL>(a, beg + gn * 32, end, lane);
         }
         const int p = beg + g * 32 + lane;
@@ -777,13 +790,16 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 // cfg 12 / 13: as cfg 0 / 8 with the sweep directions swapped (dual sweep from
 //   the chunk's end, primal from its start), so that each sweep meets the
 //   neighbours it gathers right after visiting them.
+// cfg 14 / 15: as cfg 0 / 12 in band order (all warps stride over the whole
+//   unit together instead of each block owning a contiguous chunk).
 static constexpr int TUNE_SEG = 16;
 static constexpr int N_PERSIST_CFG = 6;
 static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
-static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13;
+static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13, CFG_BAND = 14, CFG_BAND_SWAP = 15;
 static inline bool per_launch_cfg(int cfg) {
-    return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP || cfg == CFG_SWAP_PF;
+    return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP || cfg == CFG_SWAP_PF ||
+           cfg == CFG_BAND || cfg == CFG_BAND_SWAP;
 }
 static constexpr int CFG_CLUSTER8 = 10, CFG_CLUSTER16 = 11;
 static constexpr int CLUSTER_MAX_N = 1 << 17;  // cluster schedules are candidates up to this unit size
@@ -855,7 +871,8 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
     if (per_launch_cfg(cfg)) {
         const bool lean = cfg == CFG_LEAN || cfg == CFG_LEAN_PF;
         a.pf = (cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP_PF) ? 1 : 0;
-        a.swap = (cfg == CFG_SWAP || cfg == CFG_SWAP_PF) ? 1 : 0;
+        a.swap = (cfg == CFG_SWAP || cfg == CFG_SWAP_PF || cfg == CFG_BAND_SWAP) ? 1 : 0;
+        a.band = (cfg == CFG_BAND || cfg == CFG_BAND_SWAP) ? 1 : 0;
         int rc = iter_occupancy<MODE>(ctx);
         if (rc) return rc;
         for (int it = it0; it < it0 + count; ++it) {
@@ -927,7 +944,7 @@ template <int MODE>
 static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& cands) {
     int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
     if (rc) return rc;
-    cands = {0, CFG_LEAN, CFG_PF, CFG_LEAN_PF, CFG_SWAP, CFG_SWAP_PF};
+    cands = {0, CFG_LEAN, CFG_PF, CFG_LEAN_PF, CFG_SWAP, CFG_SWAP_PF, CFG_BAND, CFG_BAND_SWAP};
     int last_grid = -1;
     if (n <= (1 << 22))
         for (int k = 1; k <= N_PERSIST_CFG; ++k) {
