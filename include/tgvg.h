@@ -157,8 +157,9 @@ int tgvg_set_timing(tgvg_ctx* ctx, int on);
  * cluster of 8 / 16 CTAs running every iteration (units of at most 131072
  * cubes), 12 / 13 = as 0 / 8 with the dual sweep run from the chunk's end and
  * the primal from its start, 14 / 15 = as 0 / 12 with all warps striding over
- * the whole level together (band order), -1 = let the online autotuner choose
- * (default).  Results do not depend on it. */
+ * the whole level together (band order), 16 / 17 = as 14 / 15 with two cubes
+ * per thread and step, -1 = let the online autotuner choose (default).
+ * Results do not depend on it. */
 int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
 /* CUDA graphs for the level loop (1 = on, the default; 0 = off).  When every
  * level's schedule is already fixed (chosen by the autotuner in an earlier

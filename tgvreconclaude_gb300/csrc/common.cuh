@@ -176,6 +176,7 @@ struct tgvg_ctx {
     int coop_max[3][2] = {};           // co-resident blocks of the persistent kernel per mode / stop
     int cluster_max[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};  // usable cluster size per mode / stop (-1 unknown)
     int iter_occ[3][2][2] = {};        // blocks/SM of the sweep kernels [mode][register-capped][dual, primal]
+    int iter_occ_ilp2[3][2] = {};      // blocks/SM of the two-cubes-per-thread sweep kernels [mode][dual, primal]
     cudaEvent_t lev_ev[2 * TGVG_MAX_LEVELS] = {};  // per-level start/end
     bool graphs = true;                // capture the level loop into a CUDA graph when possible
     std::vector<uint64_t> graph_key;   // problem signature of the cached graph

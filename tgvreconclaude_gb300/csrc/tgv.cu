@@ -410,17 +410,27 @@ __device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const floa
 
 // One cube's dual ascent: p on |grad u - v| (radius alpha1) and q on |e(v)|
 // (radius alpha0), in the reference's operation order (tgv.cpp:158-189).
+// Split into the loads (dual_load) and the arithmetic and stores (dual_finish)
+// so that a warp can issue the loads of two cubes before either's stores.
 // Returns the residual contributions through dd / nd when RES.
-template <int MODE, bool RES, bool CG>
-__device__ __forceinline__ void dual_cube(const IterArgs& a, int p, double& dd, double& nd) {
-    const float4 b = ld4<CG>(a.bar + p);
+struct DualLd { float4 b, B0, B2, B4, P, Q; float q5; };
+
+template <int MODE, bool CG>
+__device__ __forceinline__ void dual_load(const IterArgs& a, int p, DualLd& L) {
+    L.b = ld4<CG>(a.bar + p);
     const int j0 = __ldg(a.nb + p), j2 = __ldg(a.nb + 2 * a.npos + p), j4 = __ldg(a.nb + 4 * a.npos + p);
-    const float4 B0 = fetch_bar<MODE, CG>(j0, b, a.bar, a.snap);
-    const float4 B2 = fetch_bar<MODE, CG>(j2, b, a.bar, a.snap);
-    const float4 B4 = fetch_bar<MODE, CG>(j4, b, a.bar, a.snap);
-    const float4 P = ld4<CG>(a.P4 + p);
-    const float4 Q = ld4<CG>(a.Q4 + p);
-    const float q5o = ld1<CG>(a.Q1 + p);
+    L.P = ld4<CG>(a.P4 + p);
+    L.Q = ld4<CG>(a.Q4 + p);
+    L.q5 = ld1<CG>(a.Q1 + p);
+    L.B0 = fetch_bar<MODE, CG>(j0, L.b, a.bar, a.snap);
+    L.B2 = fetch_bar<MODE, CG>(j2, L.b, a.bar, a.snap);
+    L.B4 = fetch_bar<MODE, CG>(j4, L.b, a.bar, a.snap);
+}
+
+template <bool RES>
+__device__ __forceinline__ void dual_finish(const IterArgs& a, int p, const DualLd& L, double& dd, double& nd) {
+    const float4 b = L.b, B0 = L.B0, B2 = L.B2, B4 = L.B4, P = L.P, Q = L.Q;
+    const float q5o = L.q5;
     float p0 = fadd(P.x, fmul(0.25f, fsub(fsub(B0.x, b.x), b.y)));
     float p1 = fadd(P.y, fmul(0.25f, fsub(fsub(B2.x, b.x), b.z)));
     float p2 = fadd(P.z, fmul(0.25f, fsub(fsub(B4.x, b.x), b.w)));
@@ -448,37 +458,60 @@ __device__ __forceinline__ void dual_cube(const IterArgs& a, int p, double& dd, 
     }
 }
 
-// One cube's primal descent: u by the prox of tot*|u - median|, v, then the
-// extrapolated bars (tgv.cpp:191-230).
 template <int MODE, bool RES, bool CG>
-__device__ __forceinline__ void primal_cube(const IterArgs& a, int p, double& dd, double& nd) {
-    const float4 U = ld4<CG>(a.uv + p);
-    const float4 P = ld4<CG>(a.P4 + p);
-    const float4 Q = ld4<CG>(a.Q4 + p);
-    const float q5 = ld1<CG>(a.Q1 + p);
-    const float2 D = __ldg(a.dat + p);
+__device__ __forceinline__ void dual_cube(const IterArgs& a, int p, double& dd, double& nd) {
+    DualLd L;
+    dual_load<MODE, CG>(a, p, L);
+    dual_finish<RES>(a, p, L, dd, nd);
+}
+
+// One cube's primal descent: u by the prox of tot*|u - median|, v, then the
+// extrapolated bars (tgv.cpp:191-230); loads (primal_load) and arithmetic and
+// stores (primal_finish) as for the dual.  Neighbours across faces 1/3/5 give
+// their p/q components, or zero when missing (streaming: also for border cubes).
+struct PrimalLd {
+    float4 U, P, Q;
+    float q5;
+    float2 D;
+    float gp10, gq10, gq13, gq14, gp31, gq31, gq33, gq35, gp52, gq52, gq54, gq55;
+};
+
+template <int MODE, bool CG>
+__device__ __forceinline__ void primal_load(const IterArgs& a, int p, PrimalLd& L) {
+    L.U = ld4<CG>(a.uv + p);
+    L.P = ld4<CG>(a.P4 + p);
+    L.Q = ld4<CG>(a.Q4 + p);
+    L.q5 = ld1<CG>(a.Q1 + p);
+    L.D = __ldg(a.dat + p);
     const int j1 = __ldg(a.nb + a.npos + p), j3 = __ldg(a.nb + 3 * a.npos + p), j5 = __ldg(a.nb + 5 * a.npos + p);
-    float gp10 = 0.f, gq10 = 0.f, gq13 = 0.f, gq14 = 0.f;
-    float gp31 = 0.f, gq31 = 0.f, gq33 = 0.f, gq35 = 0.f;
-    float gp52 = 0.f, gq52 = 0.f, gq54 = 0.f, gq55 = 0.f;
+    L.gp10 = L.gq10 = L.gq13 = L.gq14 = 0.f;
+    L.gp31 = L.gq31 = L.gq33 = L.gq35 = 0.f;
+    L.gp52 = L.gq52 = L.gq54 = L.gq55 = 0.f;
     if (j1 >= 0 && !(MODE == M_STREAM && (j1 & BORDER))) {
         const int j = j1 & POS_MASK;
         const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
-        gp10 = a4.x; gq10 = a4.w; gq13 = b4.z; gq14 = b4.w;
+        L.gp10 = a4.x; L.gq10 = a4.w; L.gq13 = b4.z; L.gq14 = b4.w;
     }
     if (j3 >= 0 && !(MODE == M_STREAM && (j3 & BORDER))) {
         const int j = j3 & POS_MASK;
         const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
-        gp31 = a4.y; gq31 = b4.x; gq33 = b4.z; gq35 = ld1<CG>(a.Q1 + j);
+        L.gp31 = a4.y; L.gq31 = b4.x; L.gq33 = b4.z; L.gq35 = ld1<CG>(a.Q1 + j);
     }
     if (j5 >= 0 && !(MODE == M_STREAM && (j5 & BORDER))) {
         const int j = j5 & POS_MASK;
         const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
-        gp52 = a4.z; gq52 = b4.y; gq54 = b4.w; gq55 = ld1<CG>(a.Q1 + j);
+        L.gp52 = a4.z; L.gq52 = b4.y; L.gq54 = b4.w; L.gq55 = ld1<CG>(a.Q1 + j);
     }
+}
+
+template <bool RES>
+__device__ __forceinline__ void primal_finish(const IterArgs& a, int p, const PrimalLd& L, double& dd, double& nd) {
+    const float4 U = L.U, P = L.P, Q = L.Q;
+    const float q5 = L.q5;
+    const float2 D = L.D;
     const float p0 = P.x, p1 = P.y, p2 = P.z;
     const float q0 = P.w, q1 = Q.x, q2 = Q.y, q3 = Q.z, q4 = Q.w;
-    const float div_p = fadd(fadd(fsub(p0, gp10), fsub(p1, gp31)), fsub(p2, gp52));
+    const float div_p = fadd(fadd(fsub(p0, L.gp10), fsub(p1, L.gp31)), fsub(p2, L.gp52));
     const float z = fadd(U.x, fmul(0.25f, div_p));
     float un;
     if (D.y < 0.0f) {
@@ -489,9 +522,9 @@ __device__ __forceinline__ void primal_cube(const IterArgs& a, int p, double& dd
         else if (diff < -D.y) un = fadd(z, D.y);
         else un = D.x;
     }
-    const float dqx = fadd(fadd(fsub(q0, gq10), fsub(q3, gq33)), fsub(q4, gq54));
-    const float dqy = fadd(fadd(fsub(q3, gq13), fsub(q1, gq31)), fsub(q5, gq55));
-    const float dqz = fadd(fadd(fsub(q4, gq14), fsub(q5, gq35)), fsub(q2, gq52));
+    const float dqx = fadd(fadd(fsub(q0, L.gq10), fsub(q3, L.gq33)), fsub(q4, L.gq54));
+    const float dqy = fadd(fadd(fsub(q3, L.gq13), fsub(q1, L.gq31)), fsub(q5, L.gq55));
+    const float dqz = fadd(fadd(fsub(q4, L.gq14), fsub(q5, L.gq35)), fsub(q2, L.gq52));
     const float vxn = fadd(U.y, fmul(0.25f, fadd(p0, dqx)));
     const float vyn = fadd(U.z, fmul(0.25f, fadd(p1, dqy)));
     const float vzn = fadd(U.w, fmul(0.25f, fadd(p2, dqz)));
@@ -503,6 +536,13 @@ __device__ __forceinline__ void primal_cube(const IterArgs& a, int p, double& dd
         dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
         nd = (double)un * un + (double)vxn * vxn + (double)vyn * vyn + (double)vzn * vzn;
     }
+}
+
+template <int MODE, bool RES, bool CG>
+__device__ __forceinline__ void primal_cube(const IterArgs& a, int p, double& dd, double& nd) {
+    PrimalLd L;
+    primal_load<MODE, CG>(a, p, L);
+    primal_finish<RES>(a, p, L, dd, nd);
 }
 
 // A block's share of one sweep over positions [beg, end): warps take 32-cube
@@ -540,7 +580,10 @@ __device__ __forceinline__ void prefetch_group(const IterArgs& a, int q0, int en
 // global warp g takes groups g, g + (all warps), ..., so that all warps work
 // on one narrow band of positions that moves through the unit and a cube's
 // neighbours are read while their lines are still in L2.
-template <int MODE, bool RES, bool STOP, bool CG, bool DUAL, bool REV>
+// With ILP = 2 a warp takes two of its groups per step and issues the loads
+// of both cubes before either's arithmetic and stores (more loads in flight
+// per warp at the same occupancy).
+template <int MODE, bool RES, bool STOP, bool CG, bool DUAL, bool REV, int ILP = 1>
 __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpAcc& wa) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int g0 = warp, gs = blockDim.x >> 5;
@@ -552,23 +595,46 @@ __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpA
     }
     const int ngroups = (end - beg + 31) >> 5;
     const bool rev = CG ? REV : (REV != (a.swap != 0));
-    for (int gi = g0; gi < ngroups; gi += gs) {
-        const int g = rev ? (ngroups - 1 - gi) : gi;
-        if (!CG && a.pf > 0 && gi + a.pf * gs < ngroups) {
+    for (int gi = g0; gi < ngroups; gi += ILP * gs) {
+        if (ILP == 1 && !CG && a.pf > 0 && gi + a.pf * gs < ngroups) {
             const int gn = rev ? (ngroups - 1 - (gi + a.pf * gs)) : gi + a.pf * gs;
             prefetch_group<DUAL>(a, beg + gn * 32, end, lane);
         }
-        const int p = beg + g * 32 + lane;
-        int slot = -1;
-        if (p < end) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
-        bool work = p < end;
-        if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
-        double dd = 0.0, nd = 0.0;
-        if (work) {
-            if (DUAL) dual_cube<MODE, RES, CG>(a, p, dd, nd);
-            else primal_cube<MODE, RES, CG>(a, p, dd, nd);
+        int pos[ILP], slot[ILP];
+        bool work[ILP];
+#pragma unroll
+        for (int u = 0; u < ILP; ++u) {
+            const int gu = gi + u * gs;
+            const int g = rev ? (ngroups - 1 - gu) : gu;
+            pos[u] = beg + g * 32 + lane;
+            work[u] = gu < ngroups && pos[u] < end;
+            slot[u] = -1;
+            if (work[u]) slot[u] = (MODE == M_STREAM) ? __ldg(a.lid + pos[u]) : a.slot0;
+            if (STOP && work[u] && MODE == M_STREAM) work[u] = __ldcg(a.done + slot[u]) == 0;
         }
-        if (RES) wa.add(work ? slot : -1, dd, nd, a.acc, DUAL ? 1 : 0, lane);
+        if (DUAL) {
+            DualLd L[ILP];
+#pragma unroll
+            for (int u = 0; u < ILP; ++u)
+                if (work[u]) dual_load<MODE, CG>(a, pos[u], L[u]);
+#pragma unroll
+            for (int u = 0; u < ILP; ++u) {
+                double dd = 0.0, nd = 0.0;
+                if (work[u]) dual_finish<RES>(a, pos[u], L[u], dd, nd);
+                if (RES) wa.add(work[u] ? slot[u] : -1, dd, nd, a.acc, 1, lane);
+            }
+        } else {
+            PrimalLd L[ILP];
+#pragma unroll
+            for (int u = 0; u < ILP; ++u)
+                if (work[u]) primal_load<MODE, CG>(a, pos[u], L[u]);
+#pragma unroll
+            for (int u = 0; u < ILP; ++u) {
+                double dd = 0.0, nd = 0.0;
+                if (work[u]) primal_finish<RES>(a, pos[u], L[u], dd, nd);
+                if (RES) wa.add(work[u] ? slot[u] : -1, dd, nd, a.acc, 0, lane);
+            }
+        }
     }
 }
 
@@ -576,24 +642,24 @@ __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpA
 // order so it starts on the cubes whose p/q the dual sweep wrote last.
 // MINB = 8 caps registers at 32 so that 64 warps fit per SM (more loads in
 // flight); MINB = 6 (the default) allows about 42.
-template <int MODE, bool RES, bool STOP, int MINB>
+template <int MODE, bool RES, bool STOP, int MINB, int ILP = 1>
 __global__ void __launch_bounds__(ITER_BLOCK, MINB) k_dual(IterArgs a) {
     if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
     const int beg = a.o + blockIdx.x * a.chunk;
     const int end = min(a.o + a.n, beg + a.chunk);
     WarpAcc wa;
-    sweep<MODE, RES, STOP, false, true, false>(a, beg, end, wa);
+    sweep<MODE, RES, STOP, false, true, false, ILP>(a, beg, end, wa);
     if (RES) wa.flush(a.acc, 1, threadIdx.x & 31);
 }
 
-template <int MODE, bool RES, bool STOP, int MINB>
+template <int MODE, bool RES, bool STOP, int MINB, int ILP = 1>
 __global__ void __launch_bounds__(ITER_BLOCK, MINB) k_primal(IterArgs a) {
     if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
     const int blk = gridDim.x - 1 - blockIdx.x;
     const int beg = a.o + blk * a.chunk;
     const int end = min(a.o + a.n, beg + a.chunk);
     WarpAcc wa;
-    sweep<MODE, RES, STOP, false, false, true>(a, beg, end, wa);
+    sweep<MODE, RES, STOP, false, false, true, ILP>(a, beg, end, wa);
     if (RES) wa.flush(a.acc, 0, threadIdx.x & 31);
 }
 
@@ -742,15 +808,19 @@ __global__ void k_unpermute(int n, const int* __restrict__ inv, const float4* __
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 template <int MODE>
-static void launch_iter(tgvg_ctx* ctx, IterArgs a, bool res, bool stop, bool dual, bool lean) {
+static void launch_iter(tgvg_ctx* ctx, IterArgs a, bool res, bool stop, bool dual, bool lean, bool ilp2) {
     // One full wave: as many blocks as fit on the GPU at once (occupancy of the
-    // plain variant), each owning an equal contiguous chunk of the unit.
-    const int occ = ctx->iter_occ[MODE][lean ? 1 : 0][dual ? 0 : 1];
+    // variant), each owning an equal contiguous chunk of the unit.
+    const int occ = ilp2 ? ctx->iter_occ_ilp2[MODE][dual ? 0 : 1] : ctx->iter_occ[MODE][lean ? 1 : 0][dual ? 0 : 1];
     const int want = std::max(1, std::min((a.n + ITER_BLOCK - 1) / ITER_BLOCK, occ * ctx->sm_count));
     a.chunk = ((a.n + want - 1) / want + 31) / 32 * 32;
     const unsigned grid = (unsigned)((a.n + a.chunk - 1) / a.chunk);
-#define TGVG_ITER(K)                                                                    \
-    if (res && stop) K<MODE, true, true, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
+#define TGVG_ITER(K)                                                                         \
+    if (ilp2 && res && stop) K<MODE, true, true, 4, 2><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a); \
+    else if (ilp2 && res) K<MODE, true, false, 4, 2><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
+    else if (ilp2 && stop) K<MODE, false, true, 4, 2><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);  \
+    else if (ilp2) K<MODE, false, false, 4, 2><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);         \
+    else if (res && stop) K<MODE, true, true, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
     else if (res) K<MODE, true, false, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);     \
     else if (stop) K<MODE, false, true, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);    \
     else if (lean) K<MODE, false, false, 8><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
@@ -772,8 +842,15 @@ static int iter_occupancy(tgvg_ctx* ctx) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v[2], k_dual<MODE, false, false, 8>, ITER_BLOCK, 0);
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v[3], k_primal<MODE, false, false, 8>, ITER_BLOCK, 0);
+    int w[2] = {0, 0};
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w[0], k_dual<MODE, false, false, 4, 2>, ITER_BLOCK, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w[1], k_primal<MODE, false, false, 4, 2>, ITER_BLOCK, 0);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy query");
     o[0] = std::max(1, v[0]); o[1] = std::max(1, v[1]); o[2] = std::max(1, v[2]); o[3] = std::max(1, v[3]);
+    ctx->iter_occ_ilp2[MODE][0] = std::max(1, w[0]);
+    ctx->iter_occ_ilp2[MODE][1] = std::max(1, w[1]);
     return TGVG_OK;
 }
 
@@ -792,14 +869,15 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 //   neighbours it gathers right after visiting them.
 // cfg 14 / 15: as cfg 0 / 12 in band order (all warps stride over the whole
 //   unit together instead of each block owning a contiguous chunk).
+// cfg 16 / 17: as cfg 14 / 15 with two cubes per thread and step (ILP 2).
 static constexpr int TUNE_SEG = 16;
 static constexpr int N_PERSIST_CFG = 6;
 static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
 static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13, CFG_BAND = 14, CFG_BAND_SWAP = 15;
+static constexpr int CFG_BAND_ILP = 16, CFG_BAND_SWAP_ILP = 17;
 static inline bool per_launch_cfg(int cfg) {
-    return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP || cfg == CFG_SWAP_PF ||
-           cfg == CFG_BAND || cfg == CFG_BAND_SWAP;
+    return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF || (cfg >= CFG_SWAP && cfg <= CFG_BAND_SWAP_ILP);
 }
 static constexpr int CFG_CLUSTER8 = 10, CFG_CLUSTER16 = 11;
 static constexpr int CLUSTER_MAX_N = 1 << 17;  // cluster schedules are candidates up to this unit size
@@ -871,8 +949,9 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
     if (per_launch_cfg(cfg)) {
         const bool lean = cfg == CFG_LEAN || cfg == CFG_LEAN_PF;
         a.pf = (cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP_PF) ? 1 : 0;
-        a.swap = (cfg == CFG_SWAP || cfg == CFG_SWAP_PF || cfg == CFG_BAND_SWAP) ? 1 : 0;
-        a.band = (cfg == CFG_BAND || cfg == CFG_BAND_SWAP) ? 1 : 0;
+        a.swap = (cfg == CFG_SWAP || cfg == CFG_SWAP_PF || cfg == CFG_BAND_SWAP || cfg == CFG_BAND_SWAP_ILP) ? 1 : 0;
+        a.band = (cfg >= CFG_BAND && cfg <= CFG_BAND_SWAP_ILP) ? 1 : 0;
+        const bool ilp2 = cfg == CFG_BAND_ILP || cfg == CFG_BAND_SWAP_ILP;
         int rc = iter_occupancy<MODE>(ctx);
         if (rc) return rc;
         for (int it = it0; it < it0 + count; ++it) {
@@ -880,9 +959,9 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
             const bool mark = timed && it % TIMING_STRIDE == 0;
             cudaEvent_t* te = mark ? &ctx->tev[3 * (it / TIMING_STRIDE)] : nullptr;
             if (mark) TGVG_CK(ctx, record_event(te[0], ctx->stream, ctx->capturing));
-            launch_iter<MODE>(ctx, a, res, stop, true, lean);
+            launch_iter<MODE>(ctx, a, res, stop, true, lean, ilp2);
             if (mark) TGVG_CK(ctx, record_event(te[1], ctx->stream, ctx->capturing));
-            launch_iter<MODE>(ctx, a, res, stop, false, lean);
+            launch_iter<MODE>(ctx, a, res, stop, false, lean, ilp2);
             if (mark) TGVG_CK(ctx, record_event(te[2], ctx->stream, ctx->capturing));
             cudaError_t le = cudaGetLastError();
             if (le != cudaSuccess) return ctx->cuda_fail(le, "iteration launch");
@@ -944,7 +1023,8 @@ template <int MODE>
 static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& cands) {
     int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
     if (rc) return rc;
-    cands = {0, CFG_LEAN, CFG_PF, CFG_LEAN_PF, CFG_SWAP, CFG_SWAP_PF, CFG_BAND, CFG_BAND_SWAP};
+    cands = {0, CFG_LEAN, CFG_PF, CFG_LEAN_PF, CFG_SWAP, CFG_SWAP_PF, CFG_BAND, CFG_BAND_SWAP, CFG_BAND_ILP,
+             CFG_BAND_SWAP_ILP};
     int last_grid = -1;
     if (n <= (1 << 22))
         for (int k = 1; k <= N_PERSIST_CFG; ++k) {
@@ -975,7 +1055,7 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
     if (rc) return rc;
     const int tuned = ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, n))];
     if (timed) {  // per-launch event timing needs one of the per-sweep-launch schedules
-        *cfg = per_launch_cfg(tuned) ? tuned : 0;
+        *cfg = per_launch_cfg(tuned) ? tuned : CFG_BAND;
         return TGVG_OK;
     }
     if (tuned >= 0) {
@@ -989,7 +1069,7 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
     std::vector<int> cands;
     if ((rc = tune_candidates<MODE>(ctx, n, stop, cands))) return rc;
     if (!stop && (int)cands.size() * TUNE_SEG * 2 <= iters) { *cfg = -1; return TGVG_OK; }
-    *cfg = n <= 65536 ? 3 : 0;  // untuned default: one cooperative launch for small units
+    *cfg = n <= 65536 ? 3 : CFG_BAND;  // untuned default: one cooperative launch for small units, else band order
     return TGVG_OK;
 }
 
