@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define TGVG_ABI_VERSION 1
+#define TGVG_ABI_VERSION 2
 
 /* ---- status codes -------------------------------------------------------- */
 #define TGVG_OK             0
@@ -124,6 +124,9 @@ typedef struct tgvg_stats {
     double kt_dual_ms, kt_primal_ms;
     double level_ms[TGVG_MAX_LEVELS];    /* device time of level slot k (init + iterations) */
     int32_t schedule[TGVG_MAX_LEVELS];   /* iteration schedule used for level slot k       */
+    int32_t kt_fused;                    /* 1: the timed level ran the fused kernel (kt_dual_ms
+                                            holds its time, kt_primal_ms 0)                  */
+    int32_t reserved;
 } tgvg_stats;
 
 typedef struct tgvg_ctx tgvg_ctx;
@@ -158,8 +161,10 @@ int tgvg_set_timing(tgvg_ctx* ctx, int on);
  * cubes), 12 / 13 = as 0 / 8 with the dual sweep run from the chunk's end and
  * the primal from its start, 14 / 15 = as 0 / 12 with all warps striding over
  * the whole level together (band order), 16 / 17 = as 14 / 15 with two cubes
- * per thread and step, -1 = let the online autotuner choose (default).
- * Results do not depend on it. */
+ * per thread and step, 18 = one fused launch per iteration over 256-cube tiles
+ * with the tile's p/q in shared memory (in-memory and streaming semantics; OC
+ * runs 14), 19 = as 18 with the tiles' streams staged by TMA bulk copies, -1 =
+ * let the online autotuner choose (default).  Results do not depend on it. */
 int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
 /* CUDA graphs for the level loop (1 = on, the default; 0 = off).  When every
  * level's schedule is already fixed (chosen by the autotuner in an earlier

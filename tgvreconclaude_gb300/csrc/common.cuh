@@ -149,6 +149,7 @@ enum BufId {
     B_T_CUBES, B_T_HISTS, B_T_UINIT, B_T_OUT, B_KEYS, B_DEPTH, B_LEAFOF, B_BUCKET, B_BCOUNT,
     B_BOFF, B_BTOT, B_PERM, B_INV, B_HKEYS, B_HMIN, B_HMAX, B_NB, B_PAR, B_UV, B_BAR, B_P4, B_Q4,
     B_Q1, B_DAT, B_SNAP, B_LID, B_LEAVES, B_ACC, B_FLAGS, B_RANGES, B_RESID, B_LVSTAT,
+    B_BARB, B_P4B, B_Q4B, B_Q1B, B_FSLOT, B_FHALO, B_FHCNT,
     // learned warm start
     B_M_X, B_M_T, B_M_IDX, B_M_Y, B_M_LEAVES, B_M_LEAFID,
     // surface extraction
@@ -177,6 +178,8 @@ struct tgvg_ctx {
     int cluster_max[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};  // usable cluster size per mode / stop (-1 unknown)
     int iter_occ[3][2][2] = {};        // blocks/SM of the sweep kernels [mode][register-capped][dual, primal]
     int iter_occ_ilp2[3][2] = {};      // blocks/SM of the two-cubes-per-thread sweep kernels [mode][dual, primal]
+    int fused_occ[3][2] = {};          // blocks/SM of the fused iteration kernels per mode [plain, TMA-staged]
+    const void* fuse_cur = nullptr;    // the fused-schedule tables of the level being run (tgv.cu), or null
     cudaEvent_t lev_ev[2 * TGVG_MAX_LEVELS] = {};  // per-level start/end
     bool graphs = true;                // capture the level loop into a CUDA graph when possible
     std::vector<uint64_t> graph_key;   // problem signature of the cached graph

@@ -789,6 +789,450 @@ __global__ void k_check(int s0, int ns, double* __restrict__ acc, int* __restric
     q[0] = q[1] = q[2] = q[3] = 0.0;
 }
 
+// ---- fused iteration (schedule 18) ------------------------------------------
+// One launch per iteration.  Blocks take 256-cube tiles of the level (grid-
+// stride over tiles, so concurrent tiles are neighbours in Morton order).  A
+// tile's dual updates go to shared memory as well as to global memory; the
+// dual updates of the tile's halo -- active cubes outside the tile that are a
+// tile cube's -x/-y/-z neighbour -- are recomputed into shared memory from the
+// same inputs their owners use, so they are bit-identical; the primal updates
+// then read every p/q they need from shared memory.  p, q and the bars are
+// ping-pong buffers (iteration k reads set k & 1 and writes the other), so no
+// block ever reads a value another block of the same launch writes.  Cubes of
+// other levels are read from set 0, which holds every finished level.
+// Per cube and iteration that is 168 B of compulsory traffic instead of the
+// two-kernel split's 204 B (p/q are not written by one kernel and re-read by
+// the next).
+constexpr int FT = 256;       // cubes per tile = threads per block
+constexpr int FH = 3 * FT;    // halo capacity per tile (three faces per cube)
+constexpr int FHASH = 2048;   // shared hash slots for building a tile's halo
+
+struct FuseArgs {
+    const float4* bar_r; float4* bar_w;
+    const float4* P4_r; float4* P4_w;
+    const float4* Q4_r; float4* Q4_w;
+    const float* Q1_r; float* Q1_w;
+    const int* slot;    // [3][npos]: primal neighbour of faces 1/3/5: tile index, FT + halo index,
+                        // -1 (none: p/q read as zero), or -(j + 2) for a cube j of another level
+    const int* halo;    // [tile][FH] halo positions
+    const int* hcount;  // [tile] halo size
+    int ntiles;
+};
+
+// Halo and neighbour slots of the level's tiles (one block per tile).
+template <int MODE>
+__global__ void __launch_bounds__(FT) k_fuse_tiles(int o, int n, int npos, const int* __restrict__ nb,
+                                                   int* __restrict__ slot, int* __restrict__ halo,
+                                                   int* __restrict__ hcount) {
+    __shared__ int hk[FHASH];
+    __shared__ short hv[FHASH];
+    __shared__ int cnt;
+    for (int k = threadIdx.x; k < FHASH; k += FT) hk[k] = -1;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    const int t = blockIdx.x, t0 = o + t * FT;
+    const int p = t0 + threadIdx.x;
+    if (p < o + n) {
+        for (int k = 0; k < 3; ++k) {
+            const int j = nb[(2 * k + 1) * npos + p];
+            int sl;
+            if (j < 0 || (MODE == M_STREAM && (j & BORDER))) {
+                sl = -1;
+            } else {
+                const int jj = j & POS_MASK;
+                if (jj < o || jj >= o + n) sl = -(jj + 2);
+                else if (jj >= t0 && jj < t0 + FT) sl = jj - t0;
+                else {
+                    unsigned h = ((unsigned)jj * 2654435761u) & (FHASH - 1);
+                    // at most 3 * FT distinct keys in FHASH > 3 * FT slots: a free or equal slot
+                    // is met within FHASH probes
+                    for (int probe = 0; probe < FHASH; ++probe) {
+                        const int prev = atomicCAS(&hk[h], -1, jj);
+                        if (prev == -1) {
+                            const int id = atomicAdd(&cnt, 1);
+                            hv[h] = (short)id;
+                            halo[(size_t)t * FH + id] = jj;
+                            break;
+                        }
+                        if (prev == jj) break;
+                        h = (h + 1) & (FHASH - 1);
+                    }
+                    sl = -3 - (int)h;  // resolved to FT + id below, once every id is written
+                }
+            }
+            slot[(size_t)k * npos + p] = sl;
+        }
+    }
+    __syncthreads();
+    if (p < o + n)
+        for (int k = 0; k < 3; ++k) {
+            int* s = slot + (size_t)k * npos + p;
+            const int sl = *s;
+            const int j = nb[(2 * k + 1) * npos + p];
+            const int jj = j & POS_MASK;
+            const bool is_halo = j >= 0 && !(MODE == M_STREAM && (j & BORDER)) && jj >= o && jj < o + n &&
+                                 !(jj >= t0 && jj < t0 + FT);
+            if (is_halo) *s = FT + hv[-3 - sl];
+        }
+    if (threadIdx.x == 0) hcount[t] = cnt;
+}
+
+// Bars of a neighbour: own value when missing, the level-start snapshot for a
+// border cube (streaming), the current set for this level's cubes, set 0 for others.
+template <int MODE>
+__device__ __forceinline__ float4 fused_bar(int j, const float4& own, const IterArgs& a, const FuseArgs& f) {
+    if (j < 0) return own;
+    if (MODE != M_INMEM && (j & BORDER)) return a.snap[j & POS_MASK];
+    return (j >= a.o && j < a.o + a.n) ? __ldcg(f.bar_r + j) : __ldcg(a.bar + j);
+}
+
+template <int MODE>
+__device__ __forceinline__ void fused_dual_load(const IterArgs& a, const FuseArgs& f, int p, DualLd& L) {
+    L.b = __ldcg(f.bar_r + p);
+    const int j0 = __ldg(a.nb + p), j2 = __ldg(a.nb + 2 * a.npos + p), j4 = __ldg(a.nb + 4 * a.npos + p);
+    L.P = __ldcg(f.P4_r + p);
+    L.Q = __ldcg(f.Q4_r + p);
+    L.q5 = __ldcg(f.Q1_r + p);
+    L.B0 = fused_bar<MODE>(j0, L.b, a, f);
+    L.B2 = fused_bar<MODE>(j2, L.b, a, f);
+    L.B4 = fused_bar<MODE>(j4, L.b, a, f);
+}
+
+// The dual arithmetic of dual_finish, results to registers.
+__device__ __forceinline__ void dual_math(const IterArgs& a, const DualLd& L, float4& Po, float4& Qo, float& q5n) {
+    const float4 b = L.b, B0 = L.B0, B2 = L.B2, B4 = L.B4, P = L.P, Q = L.Q;
+    float p0 = fadd(P.x, fmul(0.25f, fsub(fsub(B0.x, b.x), b.y)));
+    float p1 = fadd(P.y, fmul(0.25f, fsub(fsub(B2.x, b.x), b.z)));
+    float p2 = fadd(P.z, fmul(0.25f, fsub(fsub(B4.x, b.x), b.w)));
+    clip3(p0, p1, p2, a.alpha1);
+    const float e0 = fsub(B0.y, b.y);
+    const float e1 = fsub(B2.z, b.z);
+    const float e2 = fsub(B4.w, b.w);
+    const float e3 = fmul(0.5f, fsub(fadd(fsub(B2.y, b.y), B0.z), b.z));
+    const float e4 = fmul(0.5f, fsub(fadd(fsub(B4.y, b.y), B0.w), b.w));
+    const float e5 = fmul(0.5f, fsub(fadd(fsub(B4.z, b.z), B2.w), b.w));
+    float q[6] = {fadd(P.w, fmul(0.25f, e0)), fadd(Q.x, fmul(0.25f, e1)), fadd(Q.y, fmul(0.25f, e2)),
+                  fadd(Q.z, fmul(0.25f, e3)), fadd(Q.w, fmul(0.25f, e4)), fadd(L.q5, fmul(0.25f, e5))};
+    clip6(q, a.alpha0);
+    Po = make_float4(p0, p1, p2, q[0]);
+    Qo = make_float4(q[1], q[2], q[3], q[4]);
+    q5n = q[5];
+}
+
+// FP64 residual terms of one dual update (as dual_finish computes them).
+__device__ __forceinline__ void dual_res(const DualLd& L, const float4& Po, const float4& Qo, float q5n, double& dd,
+                                         double& nd) {
+    const double d0 = (double)Po.x - L.P.x, d1 = (double)Po.y - L.P.y, d2 = (double)Po.z - L.P.z;
+    const double d3 = (double)Po.w - L.P.w, d4 = (double)Qo.x - L.Q.x, d5 = (double)Qo.y - L.Q.y;
+    const double d6 = (double)Qo.z - L.Q.z, d7 = (double)Qo.w - L.Q.w, d8 = (double)q5n - L.q5;
+    dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5 + d6 * d6 + d7 * d7 + d8 * d8;
+    nd = (double)Po.x * Po.x + (double)Po.y * Po.y + (double)Po.z * Po.z + (double)Po.w * Po.w +
+         (double)Qo.x * Qo.x + (double)Qo.y * Qo.y + (double)Qo.z * Qo.z + (double)Qo.w * Qo.w + (double)q5n * q5n;
+}
+
+// The primal's neighbour p/q of faces 1/3/5 from their slots: shared memory
+// (tile or halo), zero (none / border), or set 0 of global memory (another level).
+__device__ __forceinline__ void fused_gather(const IterArgs& a, const float4* sP, const float4* sQ, const float* s5,
+                                             const int* sl, PrimalLd& L) {
+    float g[3][4];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
+        float c5 = 0.f;
+        if (sl[k] >= 0) {
+            A = sP[sl[k]]; B = sQ[sl[k]]; c5 = s5[sl[k]];
+        } else if (sl[k] <= -2) {
+            const int j = -(sl[k] + 2);
+            A = __ldcg(a.P4 + j); B = __ldcg(a.Q4 + j); c5 = __ldcg(a.Q1 + j);
+        }
+        // face 1 needs p0, q0, q3, q4; face 3: p1, q1, q3, q5; face 5: p2, q2, q4, q5
+        if (k == 0) { g[0][0] = A.x; g[0][1] = A.w; g[0][2] = B.z; g[0][3] = B.w; }
+        else if (k == 1) { g[1][0] = A.y; g[1][1] = B.x; g[1][2] = B.z; g[1][3] = c5; }
+        else { g[2][0] = A.z; g[2][1] = B.y; g[2][2] = B.w; g[2][3] = c5; }
+    }
+    L.gp10 = g[0][0]; L.gq10 = g[0][1]; L.gq13 = g[0][2]; L.gq14 = g[0][3];
+    L.gp31 = g[1][0]; L.gq31 = g[1][1]; L.gq33 = g[1][2]; L.gq35 = g[1][3];
+    L.gp52 = g[2][0]; L.gq52 = g[2][1]; L.gq54 = g[2][2]; L.gq55 = g[2][3];
+}
+
+template <int MODE, bool RES, bool STOP>
+__global__ void __launch_bounds__(FT) k_fused(IterArgs a, FuseArgs f) {
+    __shared__ float4 sP[FT + FH], sQ[FT + FH];
+    __shared__ float s5[FT + FH];
+    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
+    const int lane = threadIdx.x & 31;
+    WarpAcc wd, wp;
+    for (int t = blockIdx.x; t < f.ntiles; t += gridDim.x) {
+        const int p = a.o + t * FT + threadIdx.x;
+        bool own = p < a.o + a.n;
+        int slot = -1;
+        if (own) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
+        if (STOP && own && MODE == M_STREAM) own = __ldcg(a.done + slot) == 0;
+        // dual: the tile's own cubes
+        double dd = 0.0, nd = 0.0;
+        if (own) {
+            DualLd L;
+            fused_dual_load<MODE>(a, f, p, L);
+            float4 Po, Qo;
+            float q5n;
+            dual_math(a, L, Po, Qo, q5n);
+            f.P4_w[p] = Po; f.Q4_w[p] = Qo; f.Q1_w[p] = q5n;
+            sP[threadIdx.x] = Po; sQ[threadIdx.x] = Qo; s5[threadIdx.x] = q5n;
+            if (RES) dual_res(L, Po, Qo, q5n, dd, nd);
+        }
+        if (RES) wd.add(own ? slot : -1, dd, nd, a.acc, 1, lane);
+        // dual: the halo, recomputed (not stored globally)
+        const int nh = __ldg(f.hcount + t);
+        for (int h = threadIdx.x; h < nh; h += FT) {
+            const int q = __ldg(f.halo + (size_t)t * FH + h);
+            DualLd L;
+            fused_dual_load<MODE>(a, f, q, L);
+            float4 Po, Qo;
+            float q5n;
+            dual_math(a, L, Po, Qo, q5n);
+            sP[FT + h] = Po; sQ[FT + h] = Qo; s5[FT + h] = q5n;
+        }
+        __syncthreads();
+        // primal
+        dd = 0.0; nd = 0.0;
+        if (own) {
+            PrimalLd L;
+            L.U = __ldcg(a.uv + p);
+            L.P = sP[threadIdx.x]; L.Q = sQ[threadIdx.x]; L.q5 = s5[threadIdx.x];
+            L.D = __ldg(a.dat + p);
+            int sl[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) sl[k] = __ldg(f.slot + (size_t)k * a.npos + p);
+            fused_gather(a, sP, sQ, s5, sl, L);
+            IterArgs w = a;
+            w.bar = f.bar_w;
+            primal_finish<RES>(w, p, L, dd, nd);
+        }
+        if (RES) wp.add(own ? slot : -1, dd, nd, a.acc, 0, lane);
+        __syncthreads();
+    }
+    if (RES) { wd.flush(a.acc, 1, lane); wp.flush(a.acc, 0, lane); }
+}
+
+// ---- fused iteration with TMA staging (schedule 19) ---------------------------
+// As k_fused, with each tile's contiguous per-cube streams (bars, p/q, u/v,
+// data term, neighbour ids and slots: 25.7 KB) brought into shared memory by
+// 1-D bulk async copies (cp.async.bulk, completion counted on an mbarrier),
+// double-buffered: one thread issues tile t + 1's copies before the block works
+// on tile t.  Only neighbour bars, halo cubes and other levels' cubes are
+// read with ordinary loads.  Every mbarrier wait is bounded; a wait that runs
+// out sets the error flag, waits (bounded) for the copies in flight and ends
+// the kernel, and the solve returns TGVG_ERR_TIMEOUT.
+struct TileStage {                 // one buffer; every member starts on a 16-byte boundary
+    float4 bar[FT], P4[FT], Q4[FT], uv[FT];
+    float Q1[FT + 4];
+    int nb[3][FT + 4];             // faces 0, 2, 4
+    int sl[3][FT + 4];             // slots of faces 1, 3, 5
+    float2 dat[FT + 2];
+};
+static_assert(sizeof(TileStage) % 16 == 0, "TileStage alignment");
+struct FusedSmem {
+    TileStage st[2];
+    float4 sP[FT + FH], sQ[FT + FH];
+    float s5[FT + FH];
+    unsigned long long mbar[2];
+};
+static constexpr size_t FUSED_TMA_SMEM = sizeof(FusedSmem);
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long long* b) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(b))
+                 : "memory");
+}
+
+// Copy elements [t0, t0 + cnt) of a 4- or 8-byte array into dst: the copy
+// starts at the 16-byte boundary at or below the first element (dst is indexed
+// from `off` = the elements before it) and is rounded up to 16 bytes.  The
+// arrays carry at least 16 bytes of padding past their end.
+__device__ __forceinline__ uint32_t slice_bytes(const void* first, int es, int cnt, int& off) {
+    const uintptr_t a = (uintptr_t)first, al = a & ~(uintptr_t)15;
+    off = (int)((a - al) / es);
+    return ((uint32_t)((off + cnt) * es) + 15u) & ~15u;
+}
+__device__ __forceinline__ const void* slice_src(const void* first) {
+    return (const void*)((uintptr_t)first & ~(uintptr_t)15);
+}
+
+// Issue tile t's copies into stage buffer S (one thread).  The fence orders
+// the block's earlier ordinary reads of S (the barrier before this call made
+// them complete) before the asynchronous writes.
+__device__ __forceinline__ void stage_tile(const IterArgs& a, const FuseArgs& f, int t, TileStage& S,
+                                           unsigned long long* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const int t0 = a.o + t * FT;
+    const int cnt = min(FT, a.o + a.n - t0);
+    int off;
+    uint32_t total = 16u * cnt * 4;
+    const float* q1 = f.Q1_r + t0;
+    const uint32_t bq1 = slice_bytes(q1, 4, cnt, off);
+    total += bq1;
+    uint32_t bnb[3], bsl[3];
+    for (int k = 0; k < 3; ++k) {
+        bnb[k] = slice_bytes(a.nb + (size_t)(2 * k) * a.npos + t0, 4, cnt, off);
+        bsl[k] = slice_bytes(f.slot + (size_t)k * a.npos + t0, 4, cnt, off);
+        total += bnb[k] + bsl[k];
+    }
+    const uint32_t bdat = slice_bytes(a.dat + t0, 8, cnt, off);
+    total += bdat;
+    mbar_expect_tx(bar, total);
+    bulk_load(S.bar, f.bar_r + t0, 16u * cnt, bar);
+    bulk_load(S.P4, f.P4_r + t0, 16u * cnt, bar);
+    bulk_load(S.Q4, f.Q4_r + t0, 16u * cnt, bar);
+    bulk_load(S.uv, a.uv + t0, 16u * cnt, bar);
+    bulk_load(S.Q1, slice_src(q1), bq1, bar);
+    for (int k = 0; k < 3; ++k) {
+        bulk_load(S.nb[k], slice_src(a.nb + (size_t)(2 * k) * a.npos + t0), bnb[k], bar);
+        bulk_load(S.sl[k], slice_src(f.slot + (size_t)k * a.npos + t0), bsl[k], bar);
+    }
+    bulk_load(S.dat, slice_src(a.dat + t0), bdat, bar);
+}
+
+// Bounded wait of every thread of the block for a stage buffer; true when all
+// saw it complete.
+__device__ __forceinline__ bool stage_wait(unsigned long long* bar, uint32_t parity) {
+    bool ok = false;
+    for (int spin = 0; spin < (1 << 22) && !ok; ++spin) {
+        ok = mbar_try_wait(bar, parity);
+        if (!ok) __nanosleep(64);
+    }
+    return __syncthreads_and(ok) != 0;
+}
+
+template <int MODE, bool RES, bool STOP>
+__global__ void __launch_bounds__(FT) k_fused_tma(IterArgs a, FuseArgs f) {
+    extern __shared__ __align__(128) unsigned char dsm[];
+    FusedSmem& sm = *reinterpret_cast<FusedSmem*>(dsm);
+    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.mbar[0]);
+        mbar_init(&sm.mbar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    WarpAcc wd, wp;
+    if (threadIdx.x == 0 && (int)blockIdx.x < f.ntiles) stage_tile(a, f, blockIdx.x, sm.st[0], &sm.mbar[0]);
+    int i = 0;
+    for (int t = blockIdx.x; t < f.ntiles; t += gridDim.x, ++i) {
+        const int b = i & 1;
+        const int tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < f.ntiles) stage_tile(a, f, tn, sm.st[b ^ 1], &sm.mbar[b ^ 1]);
+        if (!stage_wait(&sm.mbar[b], (uint32_t)(i >> 1) & 1u)) {
+            if (threadIdx.x == 0) {
+                atomicOr(a.err, 4);
+                // let the copies in flight land before the block's shared memory goes away (bounded)
+                for (int spin = 0; spin < (1 << 22) && !mbar_try_wait(&sm.mbar[b], (uint32_t)(i >> 1) & 1u); ++spin)
+                    __nanosleep(64);
+                if (tn < f.ntiles)
+                    for (int spin = 0;
+                         spin < (1 << 22) && !mbar_try_wait(&sm.mbar[b ^ 1], (uint32_t)((i + 1) >> 1) & 1u); ++spin)
+                        __nanosleep(64);
+            }
+            return;
+        }
+        const TileStage& S = sm.st[b];
+        const int t0 = a.o + t * FT;
+        const int cnt = min(FT, a.o + a.n - t0);
+        const int p = t0 + threadIdx.x;
+        bool own = threadIdx.x < cnt;
+        int slot = -1;
+        if (own) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
+        if (STOP && own && MODE == M_STREAM) own = __ldcg(a.done + slot) == 0;
+        // offsets of the 4- and 8-byte slices inside their stage arrays
+        int oq1, onb[3], osl[3], odat;
+        slice_bytes(f.Q1_r + t0, 4, cnt, oq1);
+        for (int k = 0; k < 3; ++k) {
+            slice_bytes(a.nb + (size_t)(2 * k) * a.npos + t0, 4, cnt, onb[k]);
+            slice_bytes(f.slot + (size_t)k * a.npos + t0, 4, cnt, osl[k]);
+        }
+        slice_bytes(a.dat + t0, 8, cnt, odat);
+        double dd = 0.0, nd = 0.0;
+        if (own) {
+            const int x = threadIdx.x;
+            DualLd L;
+            L.b = S.bar[x]; L.P = S.P4[x]; L.Q = S.Q4[x]; L.q5 = S.Q1[oq1 + x];
+            L.B0 = fused_bar<MODE>(S.nb[0][onb[0] + x], L.b, a, f);
+            L.B2 = fused_bar<MODE>(S.nb[1][onb[1] + x], L.b, a, f);
+            L.B4 = fused_bar<MODE>(S.nb[2][onb[2] + x], L.b, a, f);
+            float4 Po, Qo;
+            float q5n;
+            dual_math(a, L, Po, Qo, q5n);
+            f.P4_w[p] = Po; f.Q4_w[p] = Qo; f.Q1_w[p] = q5n;
+            sm.sP[x] = Po; sm.sQ[x] = Qo; sm.s5[x] = q5n;
+            if (RES) dual_res(L, Po, Qo, q5n, dd, nd);
+        }
+        if (RES) wd.add(own ? slot : -1, dd, nd, a.acc, 1, lane);
+        const int nh = __ldg(f.hcount + t);
+        for (int h = threadIdx.x; h < nh; h += FT) {
+            const int q = __ldg(f.halo + (size_t)t * FH + h);
+            DualLd L;
+            fused_dual_load<MODE>(a, f, q, L);
+            float4 Po, Qo;
+            float q5n;
+            dual_math(a, L, Po, Qo, q5n);
+            sm.sP[FT + h] = Po; sm.sQ[FT + h] = Qo; sm.s5[FT + h] = q5n;
+        }
+        __syncthreads();
+        dd = 0.0; nd = 0.0;
+        if (own) {
+            const int x = threadIdx.x;
+            PrimalLd L;
+            L.U = S.uv[x];
+            L.P = sm.sP[x]; L.Q = sm.sQ[x]; L.q5 = sm.s5[x];
+            L.D = S.dat[odat + x];
+            const int sl[3] = {S.sl[0][osl[0] + x], S.sl[1][osl[1] + x], S.sl[2][osl[2] + x]};
+            fused_gather(a, sm.sP, sm.sQ, sm.s5, sl, L);
+            IterArgs w = a;
+            w.bar = f.bar_w;
+            primal_finish<RES>(w, p, L, dd, nd);
+        }
+        if (RES) wp.add(own ? slot : -1, dd, nd, a.acc, 0, lane);
+        __syncthreads();
+    }
+    if (RES) { wd.flush(a.acc, 1, lane); wp.flush(a.acc, 0, lane); }
+}
+
+// After a fused segment [it0, it0 + count): every cube whose slot ran an odd
+// number of the segment's iterations has its state in set 1; copy it to set 0.
+__global__ void k_fuse_settle(int o, int n, int it0, int count, int slot0, const int* __restrict__ lid,
+                              const int* __restrict__ iters_run, int mode, const float4* __restrict__ barB,
+                              const float4* __restrict__ P4B, const float4* __restrict__ Q4B,
+                              const float* __restrict__ Q1B, float4* __restrict__ bar, float4* __restrict__ P4,
+                              float4* __restrict__ Q4, float* __restrict__ Q1) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int p = o + t;
+    const int s = mode == M_STREAM ? lid[p] : slot0;
+    const int e = min(iters_run[s], it0 + count) - it0;
+    if (e <= 0 || !(e & 1)) return;
+    bar[p] = barB[p];
+    P4[p] = P4B[p];
+    Q4[p] = Q4B[p];
+    Q1[p] = Q1B[p];
+}
+
 __global__ void k_unpermute(int n, const int* __restrict__ inv, const float4* __restrict__ uv,
                             const float4* __restrict__ P4, const float4* __restrict__ Q4,
                             const float* __restrict__ Q1, float* __restrict__ out) {
@@ -870,12 +1314,25 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 // cfg 14 / 15: as cfg 0 / 12 in band order (all warps stride over the whole
 //   unit together instead of each block owning a contiguous chunk).
 // cfg 16 / 17: as cfg 14 / 15 with two cubes per thread and step (ILP 2).
+// cfg 18: one fused launch per iteration over 256-cube tiles (k_fused);
+//   in-memory and streaming semantics (OC semantics run cfg 14 instead).
+// cfg 19: as 18 with the tiles' contiguous streams staged by TMA bulk copies
+//   (k_fused_tma).
 static constexpr int TUNE_SEG = 16;
 static constexpr int N_PERSIST_CFG = 6;
 static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
 static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13, CFG_BAND = 14, CFG_BAND_SWAP = 15;
-static constexpr int CFG_BAND_ILP = 16, CFG_BAND_SWAP_ILP = 17;
+static constexpr int CFG_BAND_ILP = 16, CFG_BAND_SWAP_ILP = 17, CFG_FUSED = 18, CFG_FUSED_TMA = 19;
+static inline bool fused_cfg(int cfg) { return cfg == CFG_FUSED || cfg == CFG_FUSED_TMA; }
+
+// Host-side tables of the fused schedule for one level: the second (ping-pong)
+// set of bars and p/q, the neighbour slots, the tiles' halos.
+struct FuseSet {
+    float4* barB; float4* P4B; float4* Q4B; float* Q1B;
+    const int* slot; const int* halo; const int* hcount;
+    int ntiles;
+};
 static inline bool per_launch_cfg(int cfg) {
     return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF || (cfg >= CFG_SWAP && cfg <= CFG_BAND_SWAP_ILP);
 }
@@ -943,9 +1400,86 @@ static cudaError_t record_event(cudaEvent_t e, cudaStream_t s, bool capturing) {
 // Per-launch timing samples every TIMING_STRIDE-th iteration of the timed level.
 static constexpr int TIMING_STRIDE = 10;
 
+// Blocks per SM of the fused kernels (tma: the staged variant, which also gets
+// its dynamic shared memory limit raised here, before any stream capture).
+template <int MODE>
+static int fused_occupancy(tgvg_ctx* ctx, bool tma, int* out) {
+    int& o = ctx->fused_occ[MODE][tma ? 1 : 0];
+    if (o <= 0) {
+        int v = 0;
+        cudaError_t e;
+        if (tma) {
+            e = cudaSuccess;
+            const void* ks[] = {(const void*)k_fused_tma<MODE, false, false>, (const void*)k_fused_tma<MODE, true, false>,
+                                (const void*)k_fused_tma<MODE, false, true>, (const void*)k_fused_tma<MODE, true, true>};
+            for (const void* k : ks)
+                if (e == cudaSuccess)
+                    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FUSED_TMA_SMEM);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_fused_tma<MODE, false, false>, FT,
+                                                                  FUSED_TMA_SMEM);
+        } else {
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_fused<MODE, false, false>, FT, 0);
+        }
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy query");
+        o = std::max(1, v);
+    }
+    *out = o;
+    return TGVG_OK;
+}
+
 template <int MODE>
 static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, bool stop, bool timed) {
     if (count <= 0) return TGVG_OK;
+    const FuseSet* fz = static_cast<const FuseSet*>(ctx->fuse_cur);
+    if (fused_cfg(cfg) && (MODE == M_OC || !fz)) cfg = CFG_BAND;
+    if (fused_cfg(cfg)) {
+        const bool tma = cfg == CFG_FUSED_TMA;
+        int occ = 0, rc = fused_occupancy<MODE>(ctx, tma, &occ);
+        if (rc) return rc;
+        const unsigned grid = (unsigned)std::max(1, std::min(fz->ntiles, occ * ctx->sm_count));
+        for (int it = it0; it < it0 + count; ++it) {
+            const bool res = stop && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
+            const bool odd = ((it - it0) & 1) != 0;
+            FuseArgs f;
+            f.bar_r = odd ? fz->barB : a.bar; f.bar_w = odd ? a.bar : fz->barB;
+            f.P4_r = odd ? fz->P4B : a.P4;   f.P4_w = odd ? a.P4 : fz->P4B;
+            f.Q4_r = odd ? fz->Q4B : a.Q4;   f.Q4_w = odd ? a.Q4 : fz->Q4B;
+            f.Q1_r = odd ? fz->Q1B : a.Q1;   f.Q1_w = odd ? a.Q1 : fz->Q1B;
+            f.slot = fz->slot; f.halo = fz->halo; f.hcount = fz->hcount; f.ntiles = fz->ntiles;
+            const bool mark = timed && it % TIMING_STRIDE == 0;
+            cudaEvent_t* te = mark ? &ctx->tev[3 * (it / TIMING_STRIDE)] : nullptr;
+            if (mark) TGVG_CK(ctx, record_event(te[0], ctx->stream, ctx->capturing));
+            const size_t sh = tma ? FUSED_TMA_SMEM : 0;
+            if (tma) {
+                if (res && stop) k_fused_tma<MODE, true, true><<<grid, FT, sh, ctx->stream>>>(a, f);
+                else if (res) k_fused_tma<MODE, true, false><<<grid, FT, sh, ctx->stream>>>(a, f);
+                else if (stop) k_fused_tma<MODE, false, true><<<grid, FT, sh, ctx->stream>>>(a, f);
+                else k_fused_tma<MODE, false, false><<<grid, FT, sh, ctx->stream>>>(a, f);
+            } else {
+                if (res && stop) k_fused<MODE, true, true><<<grid, FT, 0, ctx->stream>>>(a, f);
+                else if (res) k_fused<MODE, true, false><<<grid, FT, 0, ctx->stream>>>(a, f);
+                else if (stop) k_fused<MODE, false, true><<<grid, FT, 0, ctx->stream>>>(a, f);
+                else k_fused<MODE, false, false><<<grid, FT, 0, ctx->stream>>>(a, f);
+            }
+            TGVG_LAUNCHED(ctx);
+            if (mark) {
+                TGVG_CK(ctx, record_event(te[1], ctx->stream, ctx->capturing));
+                TGVG_CK(ctx, record_event(te[2], ctx->stream, ctx->capturing));
+            }
+            if (res) {
+                const int ns = unit_slots<MODE>(a.nslot);
+                k_check<<<blocks_for(ns, 128), 128, 0, ctx->stream>>>(a.slot0, ns, a.acc, a.done, a.tol, it,
+                                                                          a.iters_run, a.resid);
+                TGVG_LAUNCHED(ctx);
+            }
+        }
+        k_fuse_settle<<<blocks_for(a.n, 256), 256, 0, ctx->stream>>>(a.o, a.n, it0, count, a.slot0, a.lid, a.iters_run,
+                                                                      MODE, fz->barB, fz->P4B, fz->Q4B, fz->Q1B,
+                                                                      a.bar, a.P4, a.Q4, a.Q1);
+        TGVG_LAUNCHED(ctx);
+        return TGVG_OK;
+    }
     if (per_launch_cfg(cfg)) {
         const bool lean = cfg == CFG_LEAN || cfg == CFG_LEAN_PF;
         a.pf = (cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP_PF) ? 1 : 0;
@@ -1038,6 +1572,10 @@ static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& ca
         if (cs >= 8) cands.push_back(CFG_CLUSTER8);
         if (cs >= 16) cands.push_back(CFG_CLUSTER16);
     }
+    if (MODE != M_OC && ctx->fuse_cur) {
+        cands.push_back(CFG_FUSED);
+        cands.push_back(CFG_FUSED_TMA);
+    }
     return TGVG_OK;
 }
 
@@ -1054,8 +1592,12 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
     if (!rc) rc = coop_capacity<MODE>(ctx, stop, &cmax);
     if (rc) return rc;
     const int tuned = ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, n))];
-    if (timed) {  // per-launch event timing needs one of the per-sweep-launch schedules
-        *cfg = per_launch_cfg(tuned) ? tuned : CFG_BAND;
+    if (timed) {  // per-launch event timing needs one of the per-sweep-launch or fused schedules
+        *cfg = (per_launch_cfg(tuned) || (fused_cfg(tuned) && MODE != M_OC)) ? tuned : CFG_BAND;
+        if (fused_cfg(*cfg)) {
+            int occ = 0;
+            return fused_occupancy<MODE>(ctx, *cfg == CFG_FUSED_TMA, &occ);
+        }
         return TGVG_OK;
     }
     if (tuned >= 0) {
@@ -1063,6 +1605,11 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
         if (tuned == CFG_CLUSTER8 || tuned == CFG_CLUSTER16) {  // set up before any stream capture
             int cs = 0;
             return cluster_capacity<MODE>(ctx, stop, &cs);
+        }
+        if (fused_cfg(tuned)) {
+            if (MODE == M_OC) *cfg = CFG_BAND;
+            int occ = 0;
+            return fused_occupancy<MODE>(ctx, tuned == CFG_FUSED_TMA, &occ);
         }
         return TGVG_OK;
     }
@@ -1173,14 +1720,14 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     auto* hk = (unsigned long long*)B(B_HKEYS, 8ull * cap);
     auto* hmin = (int*)B(B_HMIN, 4ull * cap);
     auto* hmax = (int*)B(B_HMAX, 4ull * cap);
-    auto* nb = (int*)B(B_NB, 4ull * 6 * n);
+    auto* nb = (int*)B(B_NB, 4ull * 6 * n + 64);  // padded: staged slices round up to 16 B
     auto* par = (int*)B(B_PAR, 4ull * n);
     auto* uv = (float4*)B(B_UV, 16ull * n);
     auto* bar = (float4*)B(B_BAR, 16ull * n);
     auto* P4 = (float4*)B(B_P4, 16ull * n);
     auto* Q4 = (float4*)B(B_Q4, 16ull * n);
-    auto* Q1 = (float*)B(B_Q1, 4ull * n);
-    auto* dat = (float2*)B(B_DAT, 8ull * n);
+    auto* Q1 = (float*)B(B_Q1, 4ull * n + 64);
+    auto* dat = (float2*)B(B_DAT, 8ull * n + 64);
     auto* snap = (float4*)B(B_SNAP, mode == M_INMEM ? 16 : 16ull * n);
     auto* lid = (int*)B(B_LID, 4ull * n);
     auto* lv = (int*)B(B_LEAVES, 4ull * (3 * std::max(1, nsl) + 2 * std::max(1, L)));
@@ -1273,6 +1820,42 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                                      ctx->stream));
         TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
     }
+    // ---- fused-schedule tables, per level (in-memory and streaming semantics)
+    std::vector<FuseSet> fsets(NBUCKET);
+    bool fused_ok = false;
+    const int fiters = std::max(0, prm->iters);
+    if (mode != M_OC && fiters > 0 && n_act > 0) {
+        int64_t total_tiles = 0;
+        for (int Ld = min_d; Ld <= max_d; ++Ld) total_tiles += (h_bstart[Ld + 1] - h_bstart[Ld] + FT - 1) / FT;
+        auto* barB = (float4*)B(B_BARB, 16ull * n);
+        auto* P4B = (float4*)B(B_P4B, 16ull * n);
+        auto* Q4B = (float4*)B(B_Q4B, 16ull * n);
+        auto* Q1B = (float*)B(B_Q1B, 4ull * n + 64);
+        auto* fslot = (int*)B(B_FSLOT, 12ull * n + 64);
+        auto* fhalo = (int*)B(B_FHALO, 4ull * FH * std::max<int64_t>(1, total_tiles));
+        auto* fhcnt = (int*)B(B_FHCNT, 4ull * std::max<int64_t>(1, total_tiles));
+        if (!barB || !P4B || !Q4B || !Q1B || !fslot || !fhalo || !fhcnt) return TGVG_ERR_NOMEM;
+        int64_t base = 0;
+        for (int Ld = min_d; Ld <= max_d; ++Ld) {
+            const int o = h_bstart[Ld], cnt = h_bstart[Ld + 1] - h_bstart[Ld];
+            if (cnt <= 0) continue;
+            const int tiles = (cnt + FT - 1) / FT;
+            if (mode == M_INMEM)
+                k_fuse_tiles<M_INMEM><<<tiles, FT, 0, ctx->stream>>>(o, cnt, n, nb, fslot, fhalo + base * FH, fhcnt + base);
+            else
+                k_fuse_tiles<M_STREAM><<<tiles, FT, 0, ctx->stream>>>(o, cnt, n, nb, fslot, fhalo + base * FH, fhcnt + base);
+            TGVG_LAUNCHED(ctx);
+            fsets[Ld] = FuseSet{barB, P4B, Q4B, Q1B, fslot, fhalo + base * FH, fhcnt + base, tiles};
+            base += tiles;
+        }
+        fused_ok = true;
+    }
+    // the level being planned or run; cleared on every return
+    struct FuseCur {
+        tgvg_ctx* c;
+        ~FuseCur() { c->fuse_cur = nullptr; }
+    } fuse_guard{ctx};
+    auto set_fuse = [&](int Ld) { ctx->fuse_cur = fused_ok ? &fsets[Ld] : nullptr; };
     TGVG_CK(ctx, cudaEventRecord(e1, ctx->stream));
 
     // ---- levels
@@ -1314,6 +1897,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
             lvl.us.push_back({0, o, cnt, 0});
         }
         for (Unit& u : lvl.us) {
+            set_fuse(Ld);
             const int rc = plan_unit(ctx, mode, u.n, iters, stop, Ld == t_level, &u.cfg);
             if (rc) return rc;
             tuning |= u.cfg < 0;
@@ -1376,6 +1960,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                 a.bar_gen = reinterpret_cast<unsigned*>(flags + 5);
                 a.err = flags + 6;
                 a.iters_run = iters_run; a.resid = resid;
+                set_fuse(Ld);
                 const int rc = run_unit(ctx, mode, a, iters, stop, Ld == t_level, u.cfg, &used_cfg);
                 if (rc) { nvtxRangePop(); return rc; }
             }
@@ -1405,7 +1990,11 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         std::memcpy(&fb[1], &prm->alpha1, 4);
         std::memcpy(&fb[2], &prm->tol, 4);
         for (uint32_t f : fb) key.push_back(f);
-        const void* ptrs[] = {nb, par, uv, bar, P4, Q4, Q1, dat, snap, lid, acc, flags, resid, lv_res};
+        const FuseSet& fz0 = fsets[levels.front().d];
+        const void* ptrs[] = {nb, par, uv, bar, P4, Q4, Q1, dat, snap, lid, acc, flags, resid, lv_res,
+                              fused_ok ? fz0.barB : nullptr, fused_ok ? fz0.P4B : nullptr,
+                              fused_ok ? fz0.Q4B : nullptr, fused_ok ? fz0.Q1B : nullptr,
+                              fused_ok ? fz0.slot : nullptr, fused_ok ? fz0.halo : nullptr};
         for (const void* q : ptrs) key.push_back((uint64_t)(uintptr_t)q);
         for (const Level& lvl : levels) {
             key.push_back(((uint64_t)lvl.d << 32) | (uint32_t)lvl.o);
@@ -1530,6 +2119,8 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         }
         st.kt_depth = t_level;
         st.kt_launches = nt;
+        for (int k = 0; k < nlv; ++k)
+            if (levels[k].d == t_level) st.kt_fused = fused_cfg(used[k]) ? 1 : 0;
         st.kt_active = h_bstart[t_level + 1] - h_bstart[t_level];
         st.kt_dual_ms = dsum;
         st.kt_primal_ms = psum;
