@@ -341,6 +341,9 @@ def run_ours(args):
     hists_t = torch.from_numpy(w.hists.view(np.int32)).cuda()
     out_t = torch.empty((n, 13), dtype=torch.float32, device="cuda")
     prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=args.iters or cfg["iters"])
+    tune_prm = prm
+    if args.tol > 0:  # time to tolerance: the stopped solves reuse the schedules a fixed-count solve tuned
+        prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=args.max_iters, tol=args.tol, check_every=10)
     mode = "stream" if cfg["chunks"] > 1 else "inmem"
     leaves = w.leaves if mode == "stream" else None
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -350,7 +353,7 @@ def run_ours(args):
     # graph (the second solve of the same problem does) that the timed steps relaunch
     for k in range(args.warmup):
         ctx.lib.tgvg_set_timing(ctx.h, int(k > 0))
-        api.tgv_solve_device(cubes_t, hists_t, out_t, leaves, mode, prm)
+        api.tgv_solve_device(cubes_t, hists_t, out_t, leaves, mode, tune_prm if k == 0 else prm)
     ctx.lib.tgvg_set_timing(ctx.h, 1)
     torch.cuda.synchronize()
     if pg:
@@ -412,14 +415,25 @@ def run_ours(args):
             hs = {"pairs_per_s_e2e": pairs / h_dt, "ms_e2e": 1e3 * h_dt, "pairs": pairs,
                   "matches_workload": bool(np.array_equal(hh, w.hists))}
 
-        # ---- CPU oracle baseline on a bounded sample (1 thread)
-        cb = {}
+        # ---- CPU oracle baseline on a bounded sample (1 thread), and the error
+        # of this package's FP32 result against an FP64 run of the same solver
+        cb, f64 = {}, {}
         if not args.skip_cpu:
             cubes_s, hists_s = cpu_sample(w, args.cpu_sample, args.cpu_iters)
             v, dt, lis = time_cpu_oracle(cubes_s, hists_s, args.cpu_iters, 1)
             cb = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "seconds": dt, "host_cores": os.cpu_count(),
                   "sample": f"{len(cubes_s)} contiguous Morton-ordered cubes of {args.workload}, {args.cpu_iters} iterations per "
                             f"level, in-memory semantics, single thread"}
+            import oracle as O
+            ref64, _ = O.tgv_solve(cubes_s, hists_s, None, "inmem", 2.0, 1.0, args.cpu_iters, fp64=True,
+                                   nthreads=os.cpu_count() or 1)
+            gpu32, _ = api.tgv_solve(cubes_s, hists_s, None, "inmem",
+                                     api.TGVParams(alpha0=2.0, alpha1=1.0, iters=args.cpu_iters))
+            du = np.abs(gpu32["u"].astype(np.float64) - ref64[:, 0])
+            bounded = np.abs(ref64[:, 0]) <= 1.0
+            f64 = {"cubes": int(len(cubes_s)), "iters_per_level": args.cpu_iters, "max_abs_du": float(du.max()),
+                   "rms_du": float(np.sqrt(np.mean(du ** 2))), "max_abs_du_bounded": float(du[bounded].max()),
+                   "what": "this package's FP32 u against the oracle's FP64 run on the same slice"}
 
         surf = {} if args.skip_surface else surface_eval(args, w, out_t)
         ws_eval = {} if args.skip_warm else warm_start_eval(args)
@@ -432,17 +446,20 @@ def run_ours(args):
             "config": {"workload": args.workload, "cubes": n, "cameras": len(w.cams),
                        "image": f"{cfg['width']}x{cfg['height']}", "max_depth": cfg["max_depth"], "nbins": nbins,
                        "iters_per_level": prm.iters, "alpha1": prm.alpha1, "alpha0": prm.alpha0,
+                       "tol": prm.tol, "check_every": prm.check_every if prm.tol > 0 else None,
                        "semantics": "tgv_minimize" if mode == "inmem" else "tgv_minimize_streaming (batched)",
                        "chunks": len(w.leaves), "levels": {int(k): int(v) for k, v in enumerate(depth_hist) if v},
                        "l2": "inputs larger than L2 (about 100 B of state per cube)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "histograms": hs, "surface": surf,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "fp64_check": f64, "histograms": hs, "surface": surf,
             "warm_start": ws_eval,
             "clocks": clk, "graph": last_st["graph"],
             "gpu_launches": int(launches), "leaf_iters_per_step": int(li_all / args.steps),
-            "levels_detail": [{"depth": d, "active": int(a), "ms": round(m, 3), "schedule": s}
-                              for d, a, m, s in zip(last_st["depth"], last_st["active"], last_st["level_ms"],
-                                                    last_st["schedule"])],
+            "levels_detail": [{"depth": d, "active": int(a), "ms": round(m, 3), "schedule": s, "iters": it,
+                               "residual": r}
+                              for d, a, m, s, it, r in zip(last_st["depth"], last_st["active"], last_st["level_ms"],
+                                                          last_st["schedule"], last_st["iters_run"],
+                                                          last_st["residual"])],
             "gen_s": round(t_gen, 1),
         }
         print(json.dumps(result), flush=True)
@@ -470,6 +487,9 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-warm", action="store_true")
     ap.add_argument("--skip-surface", action="store_true")
+    ap.add_argument("--tol", type=float, default=0.0,
+                    help="solve each level to this relative residual (time to tolerance) instead of a fixed count")
+    ap.add_argument("--max-iters", type=int, default=6000, help="iteration cap per level with --tol")
     ap.add_argument("--warm-seeds", type=int, default=6)
     ap.add_argument("--max-cubes", type=int, default=0, help="truncate the workload (profiling runs)")
     ap.add_argument("--cache", default="", help="load the workload from / save it to this .npz (profiling runs)")

@@ -354,3 +354,19 @@ def test_constant_field_is_a_fixed_point():
     h = np.zeros((len(cubes), 8), np.uint32); h[:, 5] = 7
     out, st = api.tgv_solve(cubes, h, None, "inmem", api.TGVParams(1.0, 2.0, 30))
     assert np.all(out["u"] == np.float32(0.375)) and not out["v"].any() and not out["p"].any() and not out["q"].any()
+
+
+@pytest.mark.parametrize("case", TGV_CASES)
+def test_tgv_error_against_fp64(case, oracle_lib):
+    """The FP32 result (bit-identical to the reference) against an FP64 run of
+    the same solver on the same inputs: max |du| <= 1e-4 after the same
+    iteration count."""
+    g = load_golden(case)
+    a0, a1 = (float(x) for x in g["params"])
+    for mode in ("inmem", "stream"):
+        out, _ = api.tgv_solve(g["cubes"], g["hists"], g["leaves"], mode,
+                               api.TGVParams(alpha0=a0, alpha1=a1, iters=int(g["iters"])))
+        ref64, _ = oracle_lib.tgv_solve(g["cubes"], g["hists"], g["leaves"], mode, a0, a1, int(g["iters"]), fp64=True)
+        du = np.abs(out["u"].astype(np.float64) - ref64[:, 0]).max()
+        print(case, mode, "max|du| vs FP64", du)
+        assert du <= 1e-4, (case, mode, du)
