@@ -306,6 +306,26 @@ int tgvg_mlp_grad(tgvg_ctx* ctx, tgvg_mlp* m, const uint16_t* X, const float* t,
 int tgvg_mlp_train(tgvg_ctx* ctx, tgvg_mlp* m, const uint16_t* X, const float* t, int64_t n, int32_t epochs,
                    int32_t batch, float lr, uint64_t seed, float* last_loss);
 
+/* ---- Stage 1: cubes from a depth map (reference src/octree_builder.hpp) ---- */
+/* One base depth map: K (fx, fy, cx, cy), Rt row-major 4x4 (world <- camera),
+ * width x height depths row-major (NaN / <= 0 invalid), host memory. */
+typedef struct tgvg_depthmap {
+    float fx, fy, cx, cy;
+    float rt[16];
+    int32_t width, height;
+    const float* depths;
+} tgvg_depthmap;
+/* build_cubes_from_depthmap (octree_builder.hpp:21-29, octree_builder.cpp:30-97):
+ * one cube per valid pixel with a sample radius, at the depth
+ * cube_depth_for_radius gives, sorted by Morton code (equal codes in pixel
+ * order; the reference leaves their order unspecified).  `out` may be null
+ * (count only); else it needs room for *count cubes (width*height always
+ * suffices), else TGVG_ERR_LIMIT.  The _file form writes the TGV1 file. */
+int tgvg_build_cubes(tgvg_ctx* ctx, const tgvg_depthmap* dm, const float* origin3, float r_root, tgvg_cube* out,
+                     int64_t cap, int64_t* count);
+int tgvg_build_cubes_file(tgvg_ctx* ctx, const tgvg_depthmap* dm, const float* origin3, float r_root,
+                          const char* out_path);
+
 /* ---- surface extraction (reference src/marching_cubes.hpp) -----------------
  * The u = 0 iso-surface of a TGV state as an indexed quad mesh, two triangles
  * per quad, vertices merged by the reference's 60-bit quantised position.

@@ -448,3 +448,55 @@ def obj_text(verts, faces, normals=None):
     else:
         out += ["f %d %d %d\n" % (a + 1, b + 1, c + 1) for a, b, c in np.asarray(faces, np.int64)]
     return "".join(out)
+
+
+# ------------------------------------------------------------------ Stage 1 ---
+
+class DepthMapO(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("rt", C.c_float * 16), ("width", C.c_int32), ("height", C.c_int32),
+                ("depths", C.POINTER(C.c_float))]
+
+
+def _dmo(m):
+    d = DepthMapO()
+    d.fx, d.fy, d.cx, d.cy = m["fx"], m["fy"], m["cx"], m["cy"]
+    d.rt[:] = [float(x) for x in np.asarray(m["rt"], np.float32).reshape(16)]
+    arr = np.ascontiguousarray(m["depth"], np.float32)
+    d.height, d.width = arr.shape
+    d.depths = arr.ctypes.data_as(C.POINTER(C.c_float))
+    return d, arr
+
+
+def build_cubes(m, origin, r_root):
+    """Oracle build_cubes_from_depthmap: cubes in code order, ties in pixel order."""
+    d, keep = _dmo(m)
+    o = np.ascontiguousarray(origin, np.float32)
+    L = lib()
+    L.orc_build_cubes.restype = C.c_int64
+    n = L.orc_build_cubes(C.byref(d), _ptr(o), C.c_float(r_root), None, C.c_int64(0))
+    out = np.zeros(n, CUBE_DTYPE)
+    L.orc_build_cubes(C.byref(d), _ptr(o), C.c_float(r_root), _ptr(out), C.c_int64(n))
+    return out
+
+
+def ref_build_cubes(m, origin, r_root, tmpdir=None):
+    """The reference's build_cubes_from_depthmap (through its TGV1 file)."""
+    import tempfile
+    from tgvreconclaude_gb300 import formats
+    d, keep = _refmap(m)
+    with tempfile.TemporaryDirectory(dir=tmpdir) as td:
+        p = os.path.join(td, "c.bin")
+        rc = ref().ref_build_cubes_from_depthmap(C.byref(d), C.c_float(origin[0]), C.c_float(origin[1]),
+                                                 C.c_float(origin[2]), C.c_float(r_root), p.encode())
+        assert rc == 0
+        cubes, _ = formats.load_cubes(p)
+    return cubes
+
+
+def cube_multiset(cubes):
+    """Cubes sorted by (code, depth, r_c bits): order-free comparison key."""
+    c = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    rc_bits = c["r_c"].view(np.uint32)
+    order = np.lexsort((rc_bits, c["depth"], c["lo"], c["hi"]))
+    return c[order]

@@ -677,6 +677,89 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
     return 0;
 }
 
+// ---- Stage 1: cubes from a depth map (reference src/octree_builder.cpp:11-97,
+//      src/depth_map.cpp:4-30) --------------------------------------------------
+struct DepthMapO { float fx, fy, cx, cy; float rt[16]; int32_t width, height; const float* depths; };
+
+static inline bool dm_valid(const DepthMapO& m, int u, int v) {
+    if (u < 0 || v < 0 || u >= m.width || v >= m.height) return false;
+    const float d = m.depths[size_t(v) * m.width + u];
+    return std::isfinite(d) && d > 0.0f;
+}
+// unproject: cam = ((u - cx) d / fx, (v - cy) d / fy, d, 1); world = Rt cam (row sums left to right)
+static inline void dm_unproject(const DepthMapO& m, int u, int v, float* p) {
+    const float d = m.depths[size_t(v) * m.width + u];
+    const float c[4] = {(float(u) - m.cx) * d / m.fx, (float(v) - m.cy) * d / m.fy, d, 1.0f};
+    for (int i = 0; i < 3; ++i) {
+        float acc = m.rt[4 * i] * c[0];
+        for (int k = 1; k < 4; ++k) acc = acc + m.rt[4 * i + k] * c[k];
+        p[i] = acc;
+    }
+}
+static inline float dm_radius(const DepthMapO& m, int u, int v) {
+    if (!dm_valid(m, u, v)) return 0.0f;
+    float c[3];
+    dm_unproject(m, u, v, c);
+    const int du[4] = {1, -1, 0, 0}, dv[4] = {0, 0, 1, -1};
+    float sum = 0.0f;
+    int count = 0;
+    for (int i = 0; i < 4; ++i) {
+        const int nu = u + du[i], nv = v + dv[i];
+        if (!dm_valid(m, nu, nv)) continue;
+        float q[3];
+        dm_unproject(m, nu, nv, q);
+        const float x = q[0] - c[0], y = q[1] - c[1], z = q[2] - c[2];
+        sum += std::sqrt(x * x + y * y + z * z);
+        ++count;
+    }
+    if (count == 0) return 0.0f;
+    return 0.5f * sum / count;
+}
+// cube_depth_for_radius; (int) of round(log2(y)) with the x86 result for inf/NaN (INT_MIN)
+static int depth_for_radius(float r_x, float r_root, int max_depth) {
+    if (r_x <= 0.0f) return max_depth;
+    const float l = std::round(std::log2(r_root / (r_x * 1.125f)));
+    int d = trunc_i32(l);
+    if (d < 0) d = 0;
+    if (d > max_depth) d = max_depth;
+    for (int tries = 0; tries < 3; ++tries) {
+        const float cell = r_root / static_cast<float>(1u << d);
+        if (cell >= 0.75f * r_x && cell < 1.5f * r_x) break;
+        if (cell < 0.75f * r_x) { if (d > 0) --d; else break; }
+        else { if (d < max_depth) ++d; else break; }
+    }
+    return d;
+}
+// build_cubes_from_depthmap: pixel order, then a stable sort by code.
+static void build_cubes(const DepthMapO& m, const float* o, float r_root, std::vector<Cube>& out) {
+    const float inv_2r = 1.0f / (2.0f * r_root);
+    std::vector<std::pair<uint64_t, Cube>> cs;
+    for (int v = 0; v < m.height; ++v)
+        for (int u = 0; u < m.width; ++u) {
+            if (!dm_valid(m, u, v)) continue;
+            const float r_x = dm_radius(m, u, v);
+            if (r_x <= 0.0f) continue;
+            float p[3];
+            dm_unproject(m, u, v, p);
+            const float n[3] = {(p[0] - o[0]) * inv_2r, (p[1] - o[1]) * inv_2r, (p[2] - o[2]) * inv_2r};
+            if (n[0] < 0 || n[0] >= 1 || n[1] < 0 || n[1] >= 1 || n[2] < 0 || n[2] >= 1) continue;
+            const int d = depth_for_radius(r_x, r_root, 21);
+            const uint32_t g = 1u << d;
+            uint32_t ix[3];
+            for (int k = 0; k < 3; ++k) {
+                const float f = n[k] * static_cast<float>(g);
+                uint32_t q = f >= 0.0f ? static_cast<uint32_t>(f) : 0u;  // NaN -> 0 (x86 result)
+                ix[k] = q >= g ? g - 1 : q;
+            }
+            const int sh = 21 - d;
+            const uint64_t key = encode(ix[0] << sh, ix[1] << sh, ix[2] << sh);
+            cs.push_back({key, Cube{uint32_t(key >> 32), uint32_t(key), r_x, d}});
+        }
+    std::stable_sort(cs.begin(), cs.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    out.resize(cs.size());
+    for (size_t i = 0; i < cs.size(); ++i) out[i] = cs[i].second;
+}
+
 // ---- surface extraction (reference src/marching_cubes.cpp) ------------------
 // A quad at the zero crossing of u is placed on every face pair of cubes whose
 // u changes sign; vertices are merged by a 60-bit quantised key.
@@ -1080,4 +1163,12 @@ void orc_mesh_read(void* h, float* verts, uint32_t* faces, float* normals) {
 }
 
 void orc_mesh_free(void* h) { delete static_cast<orc::SurfMesh*>(h); }
+}
+
+extern "C" int64_t orc_build_cubes(const orc::DepthMapO* m, const float* origin, float r_root, orc::Cube* out,
+                                   int64_t cap) {
+    std::vector<orc::Cube> cs;
+    orc::build_cubes(*m, origin, r_root, cs);
+    if (out && cap >= int64_t(cs.size())) std::memcpy(out, cs.data(), cs.size() * sizeof(orc::Cube));
+    return int64_t(cs.size());
 }

@@ -9,6 +9,7 @@ run where the reference is absent.
 
     python tests/golden/make_golden.py            # histogram and TGV fixtures, then
     python tests/golden/make_golden.py --mesh     # the surface fixtures (read tgv_balanced.npz)
+    python tests/golden/make_golden.py --stage1   # the Stage-1 cube fixture
 """
 from __future__ import annotations
 
@@ -99,9 +100,29 @@ def mesh_cases():
     mesh_case("rand", c, st, h, lv, (-2.0, -1.5, -1.0), 2.0)
 
 
+def stage1_case():
+    """Stage 1: the reference's build_cubes_from_depthmap on three ray-cast maps
+    of the torus (with holes)."""
+    O.build(ref=True)
+    rng = np.random.default_rng(11)
+    rig = S.sphere_rig(3, 3.0, width=96, height=72, half_fov_deg=28)
+    maps = maps_for(S.torus_scene(0.005), rig, 500)
+    for m in maps:
+        m["depth"][rng.random(m["depth"].shape) < 0.03] = np.nan
+    out = {f"cubes{k}": O.ref_build_cubes(m, (-1.5, -1.5, -1.5), 1.5) for k, m in enumerate(maps)}
+    np.savez_compressed(os.path.join(HERE, "stage1_maps.npz"), origin=np.float32([-1.5, -1.5, -1.5]),
+                        r_root=np.float32(1.5), depths=np.stack([m["depth"] for m in maps]),
+                        rt=np.stack([m["rt"] for m in maps]).astype(np.float32),
+                        fx=np.float32([m["fx"] for m in maps]), fy=np.float32([m["fy"] for m in maps]),
+                        cx=np.float32([m["cx"] for m in maps]), cy=np.float32([m["cy"] for m in maps]), **out)
+    print("stage1_maps:", [len(v) for v in out.values()], "cubes")
+
+
 def main():
     if "--mesh" in sys.argv:
         return mesh_cases()
+    if "--stage1" in sys.argv:
+        return stage1_case()
     O.build(ref=True)
     rng = np.random.default_rng(20261203)
 
@@ -138,6 +159,7 @@ def main():
     lv = S.split_leaves(len(cb), 3, rng, cb, aligned=True)
     tgv_case("balanced", cb, hb, lv, 2.0, 1.0, 40, r_root=1.5)
     mesh_cases()
+    stage1_case()
 
 
 if __name__ == "__main__":

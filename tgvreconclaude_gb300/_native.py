@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libtgvg.so")
-SOURCES = ["capi.cu", "hist.cu", "tgv.cu", "mlp.cu", "surface.cu"]
+SOURCES = ["capi.cu", "hist.cu", "tgv.cu", "mlp.cu", "surface.cu", "prep.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
@@ -78,6 +78,12 @@ class Camera(C.Structure):
     _fields_ = [("rt_inv", C.c_float * 16), ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float),
                 ("cy", C.c_float), ("width", C.c_int32), ("height", C.c_int32), ("lidar", C.c_int32),
                 ("reserved", C.c_int32)]
+
+
+class DepthMapS(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("rt", C.c_float * 16), ("width", C.c_int32), ("height", C.c_int32),
+                ("depths", C.POINTER(C.c_float))]
 
 
 class Params(C.Structure):
@@ -146,6 +152,8 @@ _SIGS = {
     "tgvg_mlp_warm_start_dev": ([P, P, P, P, C.c_int64, C.c_int32, P, C.c_int32, P], C.c_int),
     "tgvg_mlp_grad": ([P, P, P, P, C.c_int64, P, P], C.c_int),
     "tgvg_mlp_train": ([P, P, P, P, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P], C.c_int),
+    "tgvg_build_cubes": ([P, P, P, C.c_float, P, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
+    "tgvg_build_cubes_file": ([P, P, P, C.c_float, C.c_char_p], C.c_int),
     "tgvg_extract_surface": ([P, P, P, C.c_int64, P, P, C.c_float, C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "tgvg_extract_surface_leaves": ([P, P, P, P, C.c_int32, C.c_int64, P, C.c_int32, P, C.c_float,
                                      C.POINTER(C.c_void_p)], C.c_int),

@@ -76,7 +76,7 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None and a.size else None
 
 
-# ---------------------------------------------------------------- Stage 5 ---
+# ------------------------------------------------------------- depth maps ---
 
 @dataclass
 class DepthMap:
@@ -87,6 +87,53 @@ class DepthMap:
     K: np.ndarray = field(default_factory=lambda: np.eye(3, dtype=np.float32))
     Rt: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
 
+
+# ---------------------------------------------------------------- Stage 1 ---
+
+def _depthmap_struct(dm):
+    """A DepthMap, or a dict with depth/rt/fx/fy/cx/cy, as the C struct (plus
+    the array that must stay alive while it is used)."""
+    if isinstance(dm, DepthMap):
+        depth = np.ascontiguousarray(np.asarray(dm.depths, np.float32).reshape(dm.height, dm.width))
+        K = np.asarray(dm.K, np.float32)
+        fx, fy, cx, cy, rt = K[0, 0], K[1, 1], K[0, 2], K[1, 2], dm.Rt
+    else:
+        depth = np.ascontiguousarray(dm["depth"], np.float32)
+        fx, fy, cx, cy, rt = dm["fx"], dm["fy"], dm["cx"], dm["cy"], dm["rt"]
+    s = N.DepthMapS()
+    s.fx, s.fy, s.cx, s.cy = float(fx), float(fy), float(cx), float(cy)
+    s.rt[:] = [float(x) for x in np.asarray(rt, np.float32).reshape(16)]
+    s.height, s.width = depth.shape
+    s.depths = depth.ctypes.data_as(C.POINTER(C.c_float))
+    return s, depth
+
+
+def build_cubes(dm, scene_origin, r_root) -> np.ndarray:
+    """build_cubes_from_depthmap (reference src/octree_builder.hpp:21-29) on the
+    GPU: one cube per valid pixel, sorted by Morton code, equal codes in pixel
+    order.  ``dm`` is a DepthMap or a dict (depth, rt, fx, fy, cx, cy)."""
+    ctx = context()
+    s, keep = _depthmap_struct(dm)
+    o = np.ascontiguousarray(scene_origin, np.float32)
+    n = C.c_int64(0)
+    ctx.check(ctx.lib.tgvg_build_cubes(ctx.h, C.byref(s), _p(o), C.c_float(r_root), None, 0, C.byref(n)),
+              "tgvg_build_cubes")
+    out = np.zeros(n.value, F.CUBE_DTYPE)
+    ctx.check(ctx.lib.tgvg_build_cubes(ctx.h, C.byref(s), _p(o), C.c_float(r_root), _p(out), n.value, C.byref(n)),
+              "tgvg_build_cubes")
+    return out[: n.value]
+
+
+def build_cubes_file(dm, scene_origin, r_root, out_path) -> None:
+    """The same, written as a TGV1 cube file (reference src/octree_io.hpp)."""
+    ctx = context()
+    s, keep = _depthmap_struct(dm)
+    o = np.ascontiguousarray(scene_origin, np.float32)
+    ctx.check(ctx.lib.tgvg_build_cubes_file(ctx.h, C.byref(s), _p(o), C.c_float(r_root), str(out_path).encode()),
+              "tgvg_build_cubes_file")
+
+
+# ---------------------------------------------------------------- Stage 5 ---
 
 class DepthMipmap:
     """DepthMipmap (reference src/histogram.hpp:22-38).  ``build`` runs on the GPU."""

@@ -157,6 +157,9 @@ enum BufId {
     B_S_FLAGS, B_S_QIDX, B_S_SCAN, B_S_RANK, B_S_LEAF, B_S_QKEY, B_S_QPOS, B_S_QFLIP, B_S_VTK, B_S_VTF,
     B_S_SLOT, B_S_VFLAG, B_S_VID, B_S_VERTS, B_S_FACES, B_S_TN, B_S_VCNT, B_S_VSTART, B_S_VCUR, B_S_VLIST,
     B_S_NRM,
+    // Stage 1
+    B_P_DEP, B_P_KEY, B_P_RC, B_P_DPT, B_P_KEEP, B_P_POS, B_P_THR, B_P_CKEY, B_P_CIDX, B_P_SKEY, B_P_SIDX,
+    B_P_OUT, B_P_TMP,
     B_COUNT
 };
 
@@ -224,4 +227,6 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                   const tgvg_params* params, const float* d_u_init, tgvg_state* d_out,
                   tgvg_stats* stats);
 int pyramid_dims(int32_t w, int32_t h, int32_t* dims);
+// Exclusive scan of n ints on the context stream; *total receives the sum (synchronises).
+int scan_exclusive(tgvg_ctx* ctx, const int* d_in, int64_t n, int* d_out, int64_t* total);
 }  // namespace tgvg

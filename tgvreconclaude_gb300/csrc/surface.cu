@@ -119,7 +119,7 @@ __global__ void k_scan_apply(const int* __restrict__ in, int64_t n, const int* _
 }
 
 // out[i] = sum of in[0..i) for i < n; returns the total through *total (host).
-static int scan_exclusive(tgvg_ctx* ctx, const int* d_in, int64_t n, int* d_out, int64_t* total) {
+int scan_exclusive(tgvg_ctx* ctx, const int* d_in, int64_t n, int* d_out, int64_t* total) {
     *total = 0;
     if (n <= 0) return TGVG_OK;
     const int64_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;

@@ -3,8 +3,8 @@ profiler's launch list (per-kernel time and DRAM traffic).
 
     python -m tgvreconclaude_gb300.kernel_tour [--workload torus16] [--iters 20]
 
-Stages, in order: pyramids and histograms (Stage 5) from the workload's depth
-maps; the TGV solve (Stage 6) under the in-memory, OC and streaming semantics
+Stages, in order: cubes from the first depth maps (Stage 1); pyramids and
+histograms (Stage 5) from the workload's depth maps; the TGV solve (Stage 6) under the in-memory, OC and streaming semantics
 with each schedule family forced in turn (per-sweep launches, band order, two
 cubes per thread, persistent, cluster, fused, fused with TMA staging); surface
 extraction with normals; the warm-start network's features, forward pass,
@@ -30,6 +30,11 @@ def main(argv=None):
     w = W.build(a.workload, seed=0, histograms=False, max_cubes=a.max_cubes or None)
     cfg = w.cfg
     o, r = np.float32(cfg["origin"]), float(cfg["r_root"])
+    nc = 0
+    for cam, d in list(zip(w.cams, w.depths))[:4]:
+        rt = np.linalg.inv(np.asarray(cam.rt_inv[:], np.float64).reshape(4, 4)).astype(np.float32)
+        nc += len(api.build_cubes(dict(depth=d, rt=rt, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy), o, r))
+    print(f"stage 1: {nc} cubes from 4 depth maps", flush=True)
     hists = api.compute_histograms_from_maps(w.cubes, w.cams, w.depths, cfg["origin"], cfg["r_root"], cfg["nbins"])
     print(f"histograms: {len(w.cubes)} cubes x {len(w.cams)} cameras, {int(hists.sum())} votes "
           f"({time.time() - t0:.1f} s with generation)", flush=True)
