@@ -326,6 +326,33 @@ int tgvg_build_cubes(tgvg_ctx* ctx, const tgvg_depthmap* dm, const float* origin
 int tgvg_build_cubes_file(tgvg_ctx* ctx, const tgvg_depthmap* dm, const float* origin3, float r_root,
                           const char* out_path);
 
+/* ---- Stages 2 and 3: merge and 2:1 balance (reference src/merge.hpp,
+ * src/balance.hpp) ----------------------------------------------------------
+ * kway_merge (merge.hpp:6-8, merge.cpp:7-97): k code-sorted cube lists merged by
+ * code; consecutive cubes with equal (code, depth) become one cube with the
+ * mean r_c (float sum in merge order / count).  Equal codes from different
+ * lists are taken in list order; the reference's heap takes them in an
+ * unspecified order, so the results agree whenever no code occurs in two
+ * lists.  `out` may be null (count only); else it needs room for *count cubes
+ * (the total input count always suffices), else TGVG_ERR_LIMIT.  The file form
+ * reads TGV1 files (all cubes up to the end of each file, the first file's
+ * r_root) and writes one; no inputs writes an empty file with r_root 0. */
+int tgvg_merge_cubes(tgvg_ctx* ctx, const tgvg_cube* const* arrays, const int64_t* counts, int32_t k,
+                     tgvg_cube* out, int64_t cap, int64_t* count);
+int tgvg_kway_merge(tgvg_ctx* ctx, const char* const* in_paths, int32_t k, const char* out_path);
+/* balance_octree (balance.hpp:15-16, balance.cpp:60-150): the reference's
+ * bridge cubes for 2:1 balance, added in its queue order, and its output
+ * table: one cube per key depth << 60 | (code & (2^60 - 1)), with the mean r_c
+ * of the input cubes holding the key and r_root / 2^depth for a bridge.  The
+ * output cubes are decoded from the key (so codes lose bits 60..62 and depths
+ * 16..21 read as 0..5, as in the reference) and sorted by code, then depth
+ * (the reference leaves equal codes in hash-table order).  Every input cube
+ * must have depth 0..21 and a code on its depth's grid, else
+ * TGVG_ERR_INVALID.  The file form reads and writes TGV1 files. */
+int tgvg_balance_cubes(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n, float r_root, tgvg_cube* out, int64_t cap,
+                       int64_t* count);
+int tgvg_balance_octree(tgvg_ctx* ctx, const char* in_path, const char* out_path);
+
 /* ---- surface extraction (reference src/marching_cubes.hpp) -----------------
  * The u = 0 iso-surface of a TGV state as an indexed quad mesh, two triangles
  * per quad, vertices merged by the reference's 60-bit quantised position.

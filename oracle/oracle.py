@@ -500,3 +500,58 @@ def cube_multiset(cubes):
     rc_bits = c["r_c"].view(np.uint32)
     order = np.lexsort((rc_bits, c["depth"], c["lo"], c["hi"]))
     return c[order]
+
+
+# ------------------------------------------------- Stages 2 and 3 (merge, balance) ---
+
+def merge_cubes(arrays):
+    """Oracle merge of sorted cube arrays (stable in input order for equal codes)."""
+    arrs = [np.ascontiguousarray(a, CUBE_DTYPE) for a in arrays]
+    ptrs = (C.c_void_p * max(1, len(arrs)))(*[a.ctypes.data if len(a) else None for a in arrs])
+    ns = np.array([len(a) for a in arrs] or [0], np.int64)
+    L = lib()
+    L.orc_merge_cubes.restype = C.c_int64
+    n = L.orc_merge_cubes(ptrs, _ptr(ns), len(arrs), None, C.c_int64(0))
+    out = np.zeros(n, CUBE_DTYPE)
+    L.orc_merge_cubes(ptrs, _ptr(ns), len(arrs), _ptr(out), C.c_int64(n))
+    return out
+
+
+def ref_merge_cubes(arrays, r_root, tmpdir=None):
+    """The reference's kway_merge over TGV1 files holding the arrays."""
+    import tempfile
+    from tgvreconclaude_gb300 import formats
+    with tempfile.TemporaryDirectory(dir=tmpdir) as td:
+        paths = []
+        for i, a in enumerate(arrays):
+            p = os.path.join(td, f"in{i}.cubes")
+            formats.save_cubes(p, a, r_root)
+            paths.append(p)
+        out = os.path.join(td, "out.cubes")
+        arr = (C.c_char_p * max(1, len(paths)))(*[p.encode() for p in paths])
+        assert ref().ref_kway_merge(arr, len(paths), out.encode()) == 0
+        cubes, rr = formats.load_cubes(out)
+    return cubes
+
+
+def balance_cubes(cubes, r_root):
+    """Oracle 2:1 balance (output sorted by code, then depth)."""
+    c = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    L = lib()
+    L.orc_balance_cubes.restype = C.c_int64
+    n = L.orc_balance_cubes(_ptr(c), C.c_int64(len(c)), C.c_float(r_root), None, C.c_int64(0))
+    out = np.zeros(n, CUBE_DTYPE)
+    L.orc_balance_cubes(_ptr(c), C.c_int64(len(c)), C.c_float(r_root), _ptr(out), C.c_int64(n))
+    return out
+
+
+def ref_balance_cubes(cubes, r_root, tmpdir=None):
+    """The reference's balance_octree through TGV1 files."""
+    import tempfile
+    from tgvreconclaude_gb300 import formats
+    with tempfile.TemporaryDirectory(dir=tmpdir) as td:
+        p, q = os.path.join(td, "in.cubes"), os.path.join(td, "out.cubes")
+        formats.save_cubes(p, cubes, r_root)
+        assert ref().ref_balance_octree(p.encode(), q.encode()) == 0
+        out, _ = formats.load_cubes(q)
+    return out

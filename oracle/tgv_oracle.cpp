@@ -19,6 +19,7 @@
 #include <cstring>
 #include <limits>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1169,6 +1170,133 @@ extern "C" int64_t orc_build_cubes(const orc::DepthMapO* m, const float* origin,
                                    int64_t cap) {
     std::vector<orc::Cube> cs;
     orc::build_cubes(*m, origin, r_root, cs);
+    if (out && cap >= int64_t(cs.size())) std::memcpy(out, cs.data(), cs.size() * sizeof(orc::Cube));
+    return int64_t(cs.size());
+}
+
+// ---- Stage 2: merge of sorted cube arrays (reference src/merge.cpp:7-97) -----
+// The reference pops a min-heap keyed on the code alone, so when two inputs
+// hold equal codes the pop order is whatever std::priority_queue does with
+// ties.  This restatement takes them in input order (a stable merge); the two
+// agree whenever no code occurs in more than one input.  A run of consecutive
+// entries with equal (code, depth) becomes one cube whose r_c is the float sum
+// of the run in pop order divided by its length (merge.cpp:64-88); equal codes
+// of different depths that alternate are not merged, as in the reference.
+namespace orc {
+static void merge_cubes(const Cube* const* in, const int64_t* n, int k, std::vector<Cube>& out) {
+    struct Ent { uint64_t code; int src; int64_t pos; };
+    std::vector<Ent> all;
+    for (int s = 0; s < k; ++s)
+        for (int64_t i = 0; i < n[s]; ++i) all.push_back({key_of(in[s][i].hi, in[s][i].lo), s, i});
+    std::stable_sort(all.begin(), all.end(), [](const Ent& a, const Ent& b) { return a.code < b.code; });
+    out.clear();
+    float sum = 0.0f;
+    uint32_t cnt = 0;
+    for (const Ent& e : all) {
+        const Cube& c = in[e.src][e.pos];
+        if (cnt && key_of(out.back().hi, out.back().lo) == e.code && out.back().depth == c.depth) {
+            sum += c.r_c;
+            ++cnt;
+            continue;
+        }
+        if (cnt) out.back().r_c = sum / static_cast<float>(cnt);
+        out.push_back(c);
+        sum = c.r_c;
+        cnt = 1;
+    }
+    if (cnt) out.back().r_c = sum / static_cast<float>(cnt);
+}
+
+// ---- Stage 3: 2:1 balance (reference src/balance.cpp:60-150) -----------------
+// Cells are (depth, code).  Presence is tested on the exact code per depth; the
+// output table is keyed like the reference's dc_key, depth << 60 | (code & (2^60 - 1))
+// in 64-bit arithmetic (balance.cpp:57-59), so the code's top three bits are
+// dropped and depths 16..21 share keys with depths 0..5.  Output cubes are
+// decoded from that key.  Duplicate keys average their r_c in input order
+// (balance.cpp:66-75).  A FIFO of cells, seeded with every input cube in input
+// order, is processed one cell at a time: for each face whose same-depth
+// neighbour is absent, whose neighbour's parent is absent, and which has any
+// coarser ancestor present at depth <= d-2, the parent is added as a bridge with
+// r_c = r_root / 2^(d-1), unless its key is already in the output table, and is
+// queued (balance.cpp:82-121).  Cells of depth < 2 are skipped.
+struct CellHash {
+    size_t operator()(const std::pair<uint64_t, int>& c) const {
+        uint64_t h = c.first * 0x9e3779b97f4a7c15ull ^ (uint64_t(c.second) * 0xc2b2ae3d27d4eb4full);
+        return size_t(h ^ (h >> 29));
+    }
+};
+static inline uint64_t table_key(int depth, uint64_t code) {
+    return (uint64_t(uint32_t(depth)) << 60) | (code & 0x0fffffffffffffffull);
+}
+static void balance_cubes(const Cube* in, int64_t n, float r_root, std::vector<Cube>& out) {
+    std::unordered_map<uint64_t, std::pair<float, uint32_t>> table;  // key -> (r_c sum, count)
+    std::vector<uint64_t> order;                                       // keys in first-seen order
+    table.reserve(size_t(n) * 2 + 16);
+    for (int64_t i = 0; i < n; ++i) {
+        auto r = table.emplace(table_key(in[i].depth, key_of(in[i].hi, in[i].lo)), std::make_pair(0.0f, 0u));
+        if (r.second) order.push_back(r.first->first);
+        r.first->second.first += in[i].r_c;
+        r.first->second.second += 1;
+    }
+    for (size_t j = 0; j < order.size(); ++j) {
+        auto& e = table[order[j]];
+        e.first /= static_cast<float>(e.second);
+    }
+    std::unordered_set<std::pair<uint64_t, int>, CellHash> present;
+    present.reserve(size_t(n) * 2 + 16);
+    std::vector<std::pair<int, uint64_t>> fifo;
+    fifo.reserve(size_t(n) + 16);
+    for (int64_t i = 0; i < n; ++i) {
+        const uint64_t c = key_of(in[i].hi, in[i].lo);
+        present.insert({c, in[i].depth});
+        fifo.push_back({in[i].depth, c});
+    }
+    for (size_t h = 0; h < fifo.size(); ++h) {
+        const int d = fifo[h].first;
+        const uint64_t c = fifo[h].second;
+        if (d < 2) continue;
+        for (int f = 0; f < 6; ++f) {
+            const uint64_t nb = face_key(c, f, d);
+            if (is_none(nb)) continue;
+            if (present.count({nb, d})) continue;
+            const uint64_t par = ancestor(nb, d - 1);
+            if (present.count({par, d - 1})) continue;
+            bool coarser = false;
+            for (int d2 = d - 2; d2 >= 0 && !coarser; --d2) coarser = present.count({ancestor(nb, d2), d2}) != 0;
+            if (!coarser) continue;
+            auto r = table.emplace(table_key(d - 1, par),
+                                   std::make_pair(r_root / static_cast<float>(1u << (d - 1)), 1u));
+            if (!r.second) continue;
+            order.push_back(r.first->first);
+            present.insert({par, d - 1});
+            fifo.push_back({d - 1, par});
+        }
+    }
+    out.resize(order.size());
+    for (size_t j = 0; j < order.size(); ++j) {
+        const uint64_t k = order[j];
+        const uint64_t code = k & 0x0fffffffffffffffull;
+        out[j] = Cube{uint32_t(code >> 32), uint32_t(code), table[k].first, int32_t(k >> 60)};
+    }
+    // The reference sorts by code only, leaving equal codes in hash-table
+    // order; here they are ordered by depth.
+    std::stable_sort(out.begin(), out.end(), [](const Cube& a, const Cube& b) {
+        const uint64_t ka = key_of(a.hi, a.lo), kb = key_of(b.hi, b.lo);
+        return ka != kb ? ka < kb : a.depth < b.depth;
+    });
+}
+}  // namespace orc
+
+extern "C" int64_t orc_merge_cubes(const orc::Cube* const* in, const int64_t* n, int k, orc::Cube* out, int64_t cap) {
+    std::vector<orc::Cube> cs;
+    orc::merge_cubes(in, n, k, cs);
+    if (out && cap >= int64_t(cs.size())) std::memcpy(out, cs.data(), cs.size() * sizeof(orc::Cube));
+    return int64_t(cs.size());
+}
+
+extern "C" int64_t orc_balance_cubes(const orc::Cube* in, int64_t n, float r_root, orc::Cube* out, int64_t cap) {
+    std::vector<orc::Cube> cs;
+    orc::balance_cubes(in, n, r_root, cs);
     if (out && cap >= int64_t(cs.size())) std::memcpy(out, cs.data(), cs.size() * sizeof(orc::Cube));
     return int64_t(cs.size());
 }

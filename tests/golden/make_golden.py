@@ -10,6 +10,7 @@ run where the reference is absent.
     python tests/golden/make_golden.py            # histogram and TGV fixtures, then
     python tests/golden/make_golden.py --mesh     # the surface fixtures (read tgv_balanced.npz)
     python tests/golden/make_golden.py --stage1   # the Stage-1 cube fixture
+    python tests/golden/make_golden.py --octree   # the merge and balance fixture
 """
 from __future__ import annotations
 
@@ -118,7 +119,36 @@ def stage1_case():
     print("stage1_maps:", [len(v) for v in out.values()], "cubes")
 
 
+def octree_case():
+    """Stages 2 and 3: the reference's kway_merge on Stage-1 lists of four maps
+    (as given, and split into code-disjoint lists), and its balance_octree on the
+    merged list, on stress inputs and on its own test cases."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import octree_cases as OC
+    from test_stage1_oracle import stage1_maps
+    O.build(ref=True)
+    maps, origin, r_root = stage1_maps(0, n=4)
+    arrs = [O.ref_build_cubes(m, origin, r_root) for m in maps]
+    parts = OC.disjoint_parts(arrs)
+    out = {}
+    for i, a in enumerate(arrs):
+        out[f"overlap_in{i}"] = a
+    for i, a in enumerate(parts):
+        out[f"disjoint_in{i}"] = a
+    out["overlap_out"] = O.ref_merge_cubes(arrs, r_root)
+    out["disjoint_out"] = O.ref_merge_cubes(parts, r_root)
+    cases = [(out["overlap_out"], r_root)] + [(OC.balance_inputs(s), 2.0) for s in range(4)] + OC.reference_cases()
+    for i, (c, rr) in enumerate(cases):
+        out[f"bal_in{i}"] = c
+        out[f"bal_r{i}"] = np.float32(rr)
+        out[f"bal_out{i}"] = O.ref_balance_cubes(c, rr)
+    np.savez_compressed(os.path.join(HERE, "octree_cases.npz"), **out)
+    print("octree_cases:", {k: len(v) for k, v in out.items() if v.ndim})
+
+
 def main():
+    if "--octree" in sys.argv:
+        return octree_case()
     if "--mesh" in sys.argv:
         return mesh_cases()
     if "--stage1" in sys.argv:
@@ -160,6 +190,7 @@ def main():
     tgv_case("balanced", cb, hb, lv, 2.0, 1.0, 40, r_root=1.5)
     mesh_cases()
     stage1_case()
+    octree_case()
 
 
 if __name__ == "__main__":

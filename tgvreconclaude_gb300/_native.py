@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libtgvg.so")
-SOURCES = ["capi.cu", "hist.cu", "tgv.cu", "mlp.cu", "surface.cu", "prep.cu"]
+SOURCES = ["capi.cu", "hist.cu", "tgv.cu", "mlp.cu", "surface.cu", "prep.cu", "octree.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
@@ -154,6 +154,10 @@ _SIGS = {
     "tgvg_mlp_train": ([P, P, P, P, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P], C.c_int),
     "tgvg_build_cubes": ([P, P, P, C.c_float, P, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
     "tgvg_build_cubes_file": ([P, P, P, C.c_float, C.c_char_p], C.c_int),
+    "tgvg_merge_cubes": ([P, P, P, C.c_int32, P, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
+    "tgvg_kway_merge": ([P, P, C.c_int32, C.c_char_p], C.c_int),
+    "tgvg_balance_cubes": ([P, P, C.c_int64, C.c_float, P, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
+    "tgvg_balance_octree": ([P, C.c_char_p, C.c_char_p], C.c_int),
     "tgvg_extract_surface": ([P, P, P, C.c_int64, P, P, C.c_float, C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "tgvg_extract_surface_leaves": ([P, P, P, P, C.c_int32, C.c_int64, P, C.c_int32, P, C.c_float,
                                      C.POINTER(C.c_void_p)], C.c_int),

@@ -21,6 +21,9 @@ from . import formats as F
 
 # ------------------------------------------------------------------ context ---
 
+TGVG_ERR_LIMIT = -10
+
+
 class Context:
     """One CUDA stream + buffer pool on one device (tgvg_create)."""
 
@@ -116,12 +119,10 @@ def build_cubes(dm, scene_origin, r_root) -> np.ndarray:
     s, keep = _depthmap_struct(dm)
     o = np.ascontiguousarray(scene_origin, np.float32)
     n = C.c_int64(0)
-    ctx.check(ctx.lib.tgvg_build_cubes(ctx.h, C.byref(s), _p(o), C.c_float(r_root), None, 0, C.byref(n)),
+    out = np.zeros(keep.size, F.CUBE_DTYPE)  # at most one cube per pixel
+    ctx.check(ctx.lib.tgvg_build_cubes(ctx.h, C.byref(s), _p(o), C.c_float(r_root), _p(out), len(out), C.byref(n)),
               "tgvg_build_cubes")
-    out = np.zeros(n.value, F.CUBE_DTYPE)
-    ctx.check(ctx.lib.tgvg_build_cubes(ctx.h, C.byref(s), _p(o), C.c_float(r_root), _p(out), n.value, C.byref(n)),
-              "tgvg_build_cubes")
-    return out[: n.value]
+    return out[: n.value].copy()
 
 
 def build_cubes_file(dm, scene_origin, r_root, out_path) -> None:
@@ -131,6 +132,53 @@ def build_cubes_file(dm, scene_origin, r_root, out_path) -> None:
     o = np.ascontiguousarray(scene_origin, np.float32)
     ctx.check(ctx.lib.tgvg_build_cubes_file(ctx.h, C.byref(s), _p(o), C.c_float(r_root), str(out_path).encode()),
               "tgvg_build_cubes_file")
+
+
+# ------------------------------------------------------- Stages 2 and 3 ---
+
+def merge_cubes(arrays) -> np.ndarray:
+    """kway_merge (reference src/merge.hpp:6-8) over code-sorted cube arrays on
+    the GPU: merged by code (equal codes in array order), consecutive equal
+    (code, depth) collapsed with the mean r_c."""
+    ctx = context()
+    arrs = [np.ascontiguousarray(a, F.CUBE_DTYPE) for a in arrays]
+    ptrs = (C.c_void_p * max(1, len(arrs)))(*[a.ctypes.data if len(a) else None for a in arrs])
+    ns = np.array([len(a) for a in arrs] or [0], np.int64)
+    n = C.c_int64(0)
+    out = np.zeros(int(ns.sum()), F.CUBE_DTYPE)  # the merge never grows the list
+    ctx.check(ctx.lib.tgvg_merge_cubes(ctx.h, ptrs, _p(ns), len(arrs), _p(out), len(out), C.byref(n)),
+              "tgvg_merge_cubes")
+    return out[: n.value].copy()
+
+
+def kway_merge(in_paths, out_path) -> None:
+    """The file form (reference kway_merge(in_paths, out_path))."""
+    ctx = context()
+    arr = (C.c_char_p * max(1, len(in_paths)))(*[str(p).encode() for p in in_paths])
+    ctx.check(ctx.lib.tgvg_kway_merge(ctx.h, arr, len(in_paths), str(out_path).encode()), "tgvg_kway_merge")
+
+
+def balance_cubes(cubes, r_root) -> np.ndarray:
+    """balance_octree (reference src/balance.hpp:15-16) on the GPU over a cube
+    array: the reference's bridge cubes and output table, sorted by code then
+    depth."""
+    ctx = context()
+    c = np.ascontiguousarray(cubes, F.CUBE_DTYPE)
+    n = C.c_int64(0)
+    out = np.zeros(4 * len(c) + 4096, F.CUBE_DTYPE)
+    rc = ctx.lib.tgvg_balance_cubes(ctx.h, _p(c), len(c), C.c_float(r_root), _p(out), len(out), C.byref(n))
+    if rc == TGVG_ERR_LIMIT:  # more bridges than the first guess: run again with the exact size
+        out = np.zeros(n.value, F.CUBE_DTYPE)
+        rc = ctx.lib.tgvg_balance_cubes(ctx.h, _p(c), len(c), C.c_float(r_root), _p(out), len(out), C.byref(n))
+    ctx.check(rc, "tgvg_balance_cubes")
+    return out[: n.value].copy()
+
+
+def balance_octree(in_path, out_path) -> None:
+    """The file form (reference balance_octree(in_path, out_path))."""
+    ctx = context()
+    ctx.check(ctx.lib.tgvg_balance_octree(ctx.h, str(in_path).encode(), str(out_path).encode()),
+              "tgvg_balance_octree")
 
 
 # ---------------------------------------------------------------- Stage 5 ---

@@ -2,9 +2,11 @@
 profiler's launch list (per-kernel time and DRAM traffic).
 
     python -m tgvreconclaude_gb300.kernel_tour [--workload torus16] [--iters 20]
+        [--max-cubes N] [--maps K] [--cache PATH]
 
-Stages, in order: cubes from the first depth maps (Stage 1); pyramids and
-histograms (Stage 5) from the workload's depth maps; the TGV solve (Stage 6) under the in-memory, OC and streaming semantics
+Stages, in order: cubes from the first depth maps (Stage 1), their merge
+(Stage 2) and its 2:1 balance (Stage 3); pyramids and histograms (Stage 5)
+from the workload's depth maps (the first K with --maps); the TGV solve (Stage 6) under the in-memory, OC and streaming semantics
 with each schedule family forced in turn (per-sweep launches, band order, two
 cubes per thread, persistent, cluster, fused, fused with TMA staging); surface
 extraction with normals; the warm-start network's features, forward pass,
@@ -23,18 +25,23 @@ def main(argv=None):
     ap.add_argument("--workload", default="torus16")
     ap.add_argument("--iters", type=int, default=20)
     ap.add_argument("--max-cubes", type=int, default=0)
+    ap.add_argument("--maps", type=int, default=0, help="depth maps used by Stages 1-5 (0: all)")
+    ap.add_argument("--cache", default="", help="workload file: written if absent, else read (no generation)")
     a = ap.parse_args(argv)
     from . import api, workloads as W, warmstart as WS
 
     t0 = time.time()
-    w = W.build(a.workload, seed=0, histograms=False, max_cubes=a.max_cubes or None)
+    w = load_or_build(a, W)
     cfg = w.cfg
     o, r = np.float32(cfg["origin"]), float(cfg["r_root"])
-    nc = 0
+    arrs = []
     for cam, d in list(zip(w.cams, w.depths))[:4]:
         rt = np.linalg.inv(np.asarray(cam.rt_inv[:], np.float64).reshape(4, 4)).astype(np.float32)
-        nc += len(api.build_cubes(dict(depth=d, rt=rt, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy), o, r))
-    print(f"stage 1: {nc} cubes from 4 depth maps", flush=True)
+        arrs.append(api.build_cubes(dict(depth=d, rt=rt, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy), o, r))
+    merged = api.merge_cubes(arrs)
+    bal = api.balance_cubes(merged, r)
+    print(f"stages 1-3: {sum(map(len, arrs))} cubes from {len(arrs)} depth maps, {len(merged)} merged, "
+          f"{len(bal)} balanced", flush=True)
     hists = api.compute_histograms_from_maps(w.cubes, w.cams, w.depths, cfg["origin"], cfg["r_root"], cfg["nbins"])
     print(f"histograms: {len(w.cubes)} cubes x {len(w.cams)} cameras, {int(hists.sum())} votes "
           f"({time.time() - t0:.1f} s with generation)", flush=True)
@@ -68,6 +75,32 @@ def main(argv=None):
     loss, _ = m.grad(X[:65536], t[:65536])
     m.train(X[:65536], t[:65536], epochs=1, batch=4096, lr=1e-4, seed=0)
     print(f"warm start: {len(u0)} predictions, loss {loss:.3g}, one training epoch", flush=True)
+
+
+def load_or_build(a, W):
+    """The workload, with its depth maps and cameras (the first --maps of them)."""
+    import os
+    from . import _native as N
+    if a.cache and os.path.exists(a.cache):
+        d = np.load(a.cache)
+        w = W.Workload(str(d["name"]), dict(W.CONFIGS[str(d["name"])]), [], list(d["depths"]), d["cubes"],
+                       d["hists"], d["leaves"], {})
+        for row in d["cams"]:
+            cam = N.Camera()
+            cam.rt_inv[:] = [float(v) for v in row[:16]]
+            cam.fx, cam.fy, cam.cx, cam.cy = (float(v) for v in row[16:20])
+            cam.width, cam.height, cam.lidar = int(row[20]), int(row[21]), int(row[22])
+            w.cams.append(cam)
+        return w
+    w = W.build(a.workload, seed=0, histograms=False, max_cubes=a.max_cubes or None)
+    if a.maps:
+        w.cams, w.depths = w.cams[:a.maps], w.depths[:a.maps]
+    if a.cache:
+        cams = np.array([list(c.rt_inv) + [c.fx, c.fy, c.cx, c.cy, c.width, c.height, c.lidar] for c in w.cams],
+                        np.float64)
+        np.savez(a.cache, name=w.name, cubes=w.cubes, hists=w.hists, leaves=w.leaves, depths=np.stack(w.depths),
+                 cams=cams)
+    return w
 
 
 if __name__ == "__main__":
