@@ -1,6 +1,7 @@
-"""The C++ drop-in (tgvreconclaude_gb300/dropin/tgv_dropin.cpp, surface_dropin.cpp)
-compiles against the reference's own headers and links into the reference's own
-Stage-5/6 test programs in place of src/histogram.cpp and src/tgv.cpp; the
+"""The C++ drop-in (tgvreconclaude_gb300/dropin/tgv_dropin.cpp, surface_dropin.cpp,
+octree_dropin.cpp) compiles against the reference's own headers and links into the
+reference's own Stage-1, 2-4, 5 and 6 test programs in place of src/histogram.cpp,
+src/tgv.cpp, src/octree_builder.cpp, src/merge.cpp and src/balance.cpp; the
 Stage-7 replacement of src/marching_cubes.cpp compiles against the reference's
 header (its test program also needs src/qslim.cpp, hence a full Eigen).  Needs the reference
 checkout; without a GPU the programs must stop at their first call with the
@@ -23,7 +24,8 @@ def test_dropin_links_reference_tests():
     _native.build()
     r = subprocess.run(["make", "-s", "-C", DROPIN, f"REF_DIR={REF_DIR}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    for t in ("test_stage5_dropin", "test_stage6_dropin", "obj/surface_dropin.o"):
+    for t in ("test_stage1_dropin", "test_stages2_4_dropin", "test_stage5_dropin", "test_stage6_dropin",
+              "obj/surface_dropin.o", "obj/octree_dropin.o"):
         assert os.path.exists(os.path.join(DROPIN, "_build", t))
 
 

@@ -98,3 +98,22 @@ def test_stages_1_to_3_at_scale(oracle_lib):
     bal = api.balance_cubes(merged, r_root)
     assert bal.tobytes() == oracle_lib.balance_cubes(merged, r_root).tobytes()
     assert len(bal) >= len(np.unique(F.cube_keys(merged)))
+
+
+def test_reference_merge_kat(tmp_path):
+    """tests/test_stages2_4.cpp:102-130: Stage-1 files of two 8x8 planes at z = 5
+    and z = 6 merge into one sorted file holding every cube of both."""
+    K = np.array([[50, 0, 4], [0, 50, 4], [0, 0, 1]], np.float32)
+    paths = []
+    for z in (5.0, 6.0):
+        dm = api.DepthMap(8, 8, np.full(64, z, np.float32), K, np.eye(4, dtype=np.float32))
+        p = tmp_path / f"z{z}.cubes"
+        api.build_cubes_file(dm, (-1.5, -1.5, 4.0), 3.0, p)
+        paths.append(p)
+    api.kway_merge(paths, tmp_path / "m.cubes")
+    m, rr = F.load_cubes(str(tmp_path / "m.cubes"))
+    a, _ = F.load_cubes(str(paths[0]))
+    b, _ = F.load_cubes(str(paths[1]))
+    k = F.cube_keys(m)
+    assert rr == 3.0 and len(m) > 0 and np.all(k[1:] >= k[:-1])
+    assert len(m) == len(a) + len(b)

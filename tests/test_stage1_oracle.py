@@ -72,3 +72,16 @@ def test_build_cubes_matches_golden(oracle_lib):
         out = oracle_lib.build_cubes(m, g["origin"], float(g["r_root"]))
         ref = g[f"cubes{k}"]
         assert oracle_lib.cube_multiset(out).tobytes() == oracle_lib.cube_multiset(ref).tobytes()
+
+
+def test_reference_build_kat(oracle_lib):
+    """tests/test_stage1.cpp:84-117 on the oracle: sorted cubes whose depths
+    satisfy 0.75 r_c <= r_root / 2^d < 1.5 r_c."""
+    m = dict(depth=np.full((10, 10), 5.0, np.float32), rt=np.eye(4, dtype=np.float32), fx=np.float32(50),
+             fy=np.float32(50), cx=np.float32(5), cy=np.float32(5))
+    cubes = oracle_lib.build_cubes(m, (-1.0, -1.0, 4.0), 2.5)
+    assert len(cubes) > 0
+    k = (cubes["hi"].astype(np.uint64) << np.uint64(32)) | cubes["lo"]
+    assert np.all(k[1:] >= k[:-1])
+    cell = np.float32(2.5) / (np.uint32(1) << cubes["depth"].astype(np.uint32)).astype(np.float32)
+    assert np.all(cell >= np.float32(0.75) * cubes["r_c"]) and np.all(cell < np.float32(1.5) * cubes["r_c"])
