@@ -288,6 +288,61 @@ def surface_eval(args, w, out_t):
     return res
 
 
+def stages13_eval(args, w):
+    """Stages 1-3 on the workload's depth maps through the host-buffer C ABI
+    calls: cubes from every map, their merge, and the 2:1 balance of the merged
+    list; the CPU oracle, and a GPU/oracle equality check, on the first two maps."""
+    from tgvreconclaude_gb300 import api
+    if not w.depths:
+        return {"unavailable": "workload loaded from a cache without depth maps"}
+    o, r = np.float32(w.cfg["origin"]), float(w.cfg["r_root"])
+
+    def as_map(cam, d):
+        rt = np.linalg.inv(np.asarray(cam.rt_inv[:], np.float64).reshape(4, 4)).astype(np.float32)
+        return dict(depth=d, rt=rt, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy)
+
+    maps = [as_map(c, d) for c, d in zip(w.cams, w.depths)]
+    api.build_cubes(maps[0], o, r)  # warm-up
+    t0 = time.perf_counter()
+    arrs = [api.build_cubes(m, o, r) for m in maps]
+    t1 = time.perf_counter()
+    merged = api.merge_cubes(arrs)
+    t2 = time.perf_counter()
+    bal = api.balance_cubes(merged, r)
+    t3 = time.perf_counter()
+    px = int(sum(m["depth"].size for m in maps))
+    n1 = int(sum(len(a) for a in arrs))
+    res = {"maps": len(maps), "pixels": px, "stage1_cubes": n1, "merged": int(len(merged)), "balanced": int(len(bal)),
+           "ms_e2e": {"stage1": 1e3 * (t1 - t0), "merge": 1e3 * (t2 - t1), "balance": 1e3 * (t3 - t2)},
+           "stage1_pixels_per_s_e2e": px / (t1 - t0), "merge_cubes_per_s_e2e": n1 / (t2 - t1),
+           "balance_cubes_per_s_e2e": len(merged) / (t3 - t2),
+           "what": "build_cubes per map, merge_cubes, balance_cubes; host arrays in and out"}
+    if not args.skip_cpu:
+        sys.path.insert(0, os.path.join(HERE, "oracle"))
+        import oracle as O
+        s_maps = maps[:2]
+        c0 = time.perf_counter()
+        s_arrs = [O.build_cubes(m, o, r) for m in s_maps]
+        c1 = time.perf_counter()
+        s_merged = O.merge_cubes(s_arrs)
+        c2 = time.perf_counter()
+        s_bal = O.balance_cubes(s_merged, r)
+        c3 = time.perf_counter()
+        s_px = int(sum(m["depth"].size for m in s_maps))
+        g_arrs = [api.build_cubes(m, o, r) for m in s_maps]
+        g_merged = api.merge_cubes(g_arrs)
+        same = (all(a.tobytes() == b.tobytes() for a, b in zip(g_arrs, s_arrs))
+                and g_merged.tobytes() == s_merged.tobytes()
+                and api.balance_cubes(g_merged, r).tobytes() == s_bal.tobytes())
+        res["cpu_baseline"] = {
+            "stage1_pixels_per_s": s_px / (c1 - c0),
+            "merge_cubes_per_s": sum(map(len, s_arrs)) / (c2 - c1),
+            "balance_cubes_per_s": len(s_merged) / (c3 - c2), "cores": 1, "kind": "port",
+            "sample": f"the first 2 depth maps of {args.workload} ({s_px} pixels, {len(s_merged)} merged cubes)"}
+        res["matches_oracle_on_sample"] = bool(same)
+    return res
+
+
 def warm_start_eval(args):
     """Time to relative residual 1e-4 (at most 6000 iterations per level) on
     held-out small scenes: zero start, trained network, reference initialisation."""
@@ -436,6 +491,7 @@ def run_ours(args):
                    "what": "this package's FP32 u against the oracle's FP64 run on the same slice"}
 
         surf = {} if args.skip_surface else surface_eval(args, w, out_t)
+        s13 = {} if args.skip_stages13 else stages13_eval(args, w)
         ws_eval = {} if args.skip_warm else warm_start_eval(args)
 
         depth_hist = np.bincount(w.cubes["depth"], minlength=22)
@@ -452,6 +508,7 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (about 100 B of state per cube)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "fp64_check": f64, "histograms": hs, "surface": surf,
+            "stages_1_3": s13,
             "warm_start": ws_eval,
             "clocks": clk, "graph": last_st["graph"],
             "gpu_launches": int(launches), "leaf_iters_per_step": int(li_all / args.steps),
@@ -487,6 +544,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-warm", action="store_true")
     ap.add_argument("--skip-surface", action="store_true")
+    ap.add_argument("--skip-stages13", action="store_true")
     ap.add_argument("--tol", type=float, default=0.0,
                     help="solve each level to this relative residual (time to tolerance) instead of a fixed count")
     ap.add_argument("--max-iters", type=int, default=6000, help="iteration cap per level with --tol")
