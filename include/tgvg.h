@@ -163,10 +163,8 @@ int tgvg_set_timing(tgvg_ctx* ctx, int on);
  * the whole level together (band order), 16 / 17 = as 14 / 15 with two cubes
  * per thread and step, 18 = one fused launch per iteration over 256-cube tiles
  * with the tile's p/q in shared memory (in-memory and streaming semantics; OC
- * runs 14), 19 = as 18 with the tiles' streams staged by TMA bulk copies,
- * 20 / 21 = as 14 with each cube's own records loaded (20) or loaded and stored
- * (21) evict-first, -1 = let the online autotuner choose (default).  Results do
- * not depend on it. */
+ * runs 14), 19 = as 18 with the tiles' streams staged by TMA bulk copies, -1 =
+ * let the online autotuner choose (default).  Results do not depend on it. */
 int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
 /* CUDA graphs for the level loop (1 = on, the default; 0 = off).  When every
  * level's schedule is already fixed (chosen by the autotuner in an earlier

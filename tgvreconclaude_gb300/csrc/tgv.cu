@@ -343,7 +343,6 @@ struct IterArgs {
     int pf;               // per-launch schedules: L2 prefetch of the warp's next group (0 = off)
     int swap;             // per-launch schedules: dual sweep in reverse order, primal forward
     int band;             // per-launch schedules: warps stride over the whole unit (grid-stride band)
-    int hint;             // per-launch schedules: own-record loads evict-first (1), and stores too (2)
 };
 
 // Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
@@ -401,28 +400,6 @@ __device__ __forceinline__ void clip6(float* q, float r) {
 template <bool CG> __device__ __forceinline__ float4 ld4(const float4* p) { return CG ? __ldcg(p) : *p; }
 template <bool CG> __device__ __forceinline__ float ld1(const float* p) { return CG ? __ldcg(p) : *p; }
 
-// A cube's own records, which no later cube of the sweep reads again (the
-// cubes that gather them come earlier in the sweep order of schedules 20/21).
-// With hint the loads are cache-streaming (ld.global.cs, evict first), and with
-// hint == 2 the stores too (st.global.cs), so that L2 keeps the lines that
-// neighbours gather.  The values are the same either way.
-template <bool CG> __device__ __forceinline__ float4 own4(const float4* p, int hint) {
-    return CG ? __ldcg(p) : (hint ? __ldcs(p) : *p);
-}
-template <bool CG> __device__ __forceinline__ float own1(const float* p, int hint) {
-    return CG ? __ldcg(p) : (hint ? __ldcs(p) : *p);
-}
-__device__ __forceinline__ int own_idx(const int* p, int hint) { return hint ? __ldcs(p) : __ldg(p); }
-__device__ __forceinline__ float2 own2(const float2* p, int hint) { return hint ? __ldcs(p) : __ldg(p); }
-__device__ __forceinline__ void put4(float4* p, float4 v, int hint) {
-    if (hint == 2) __stcs(p, v);
-    else *p = v;
-}
-__device__ __forceinline__ void put1(float* p, float v, int hint) {
-    if (hint == 2) __stcs(p, v);
-    else *p = v;
-}
-
 template <int MODE, bool CG>
 __device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const float4* __restrict__ bar,
                                             const float4* __restrict__ snap) {
@@ -440,12 +417,11 @@ struct DualLd { float4 b, B0, B2, B4, P, Q; float q5; };
 
 template <int MODE, bool CG>
 __device__ __forceinline__ void dual_load(const IterArgs& a, int p, DualLd& L) {
-    L.b = own4<CG>(a.bar + p, a.hint);
-    const int j0 = own_idx(a.nb + p, a.hint), j2 = own_idx(a.nb + 2 * a.npos + p, a.hint),
-              j4 = own_idx(a.nb + 4 * a.npos + p, a.hint);
-    L.P = own4<CG>(a.P4 + p, a.hint);
-    L.Q = own4<CG>(a.Q4 + p, a.hint);
-    L.q5 = own1<CG>(a.Q1 + p, a.hint);
+    L.b = ld4<CG>(a.bar + p);
+    const int j0 = __ldg(a.nb + p), j2 = __ldg(a.nb + 2 * a.npos + p), j4 = __ldg(a.nb + 4 * a.npos + p);
+    L.P = ld4<CG>(a.P4 + p);
+    L.Q = ld4<CG>(a.Q4 + p);
+    L.q5 = ld1<CG>(a.Q1 + p);
     L.B0 = fetch_bar<MODE, CG>(j0, L.b, a.bar, a.snap);
     L.B2 = fetch_bar<MODE, CG>(j2, L.b, a.bar, a.snap);
     L.B4 = fetch_bar<MODE, CG>(j4, L.b, a.bar, a.snap);
@@ -468,9 +444,9 @@ __device__ __forceinline__ void dual_finish(const IterArgs& a, int p, const Dual
     float q[6] = {fadd(P.w, fmul(0.25f, e0)), fadd(Q.x, fmul(0.25f, e1)), fadd(Q.y, fmul(0.25f, e2)),
                   fadd(Q.z, fmul(0.25f, e3)), fadd(Q.w, fmul(0.25f, e4)), fadd(q5o, fmul(0.25f, e5))};
     clip6(q, a.alpha0);
-    put4(a.P4 + p, make_float4(p0, p1, p2, q[0]), a.hint);
-    put4(a.Q4 + p, make_float4(q[1], q[2], q[3], q[4]), a.hint);
-    put1(a.Q1 + p, q[5], a.hint);
+    a.P4[p] = make_float4(p0, p1, p2, q[0]);
+    a.Q4[p] = make_float4(q[1], q[2], q[3], q[4]);
+    a.Q1[p] = q[5];
     if (RES) {
         const double d0 = (double)p0 - P.x, d1 = (double)p1 - P.y, d2 = (double)p2 - P.z;
         const double d3 = (double)q[0] - P.w, d4 = (double)q[1] - Q.x, d5 = (double)q[2] - Q.y;
@@ -502,13 +478,12 @@ struct PrimalLd {
 
 template <int MODE, bool CG>
 __device__ __forceinline__ void primal_load(const IterArgs& a, int p, PrimalLd& L) {
-    L.U = own4<CG>(a.uv + p, a.hint);
-    L.P = own4<CG>(a.P4 + p, a.hint);
-    L.Q = own4<CG>(a.Q4 + p, a.hint);
-    L.q5 = own1<CG>(a.Q1 + p, a.hint);
-    L.D = own2(a.dat + p, a.hint);
-    const int j1 = own_idx(a.nb + a.npos + p, a.hint), j3 = own_idx(a.nb + 3 * a.npos + p, a.hint),
-              j5 = own_idx(a.nb + 5 * a.npos + p, a.hint);
+    L.U = ld4<CG>(a.uv + p);
+    L.P = ld4<CG>(a.P4 + p);
+    L.Q = ld4<CG>(a.Q4 + p);
+    L.q5 = ld1<CG>(a.Q1 + p);
+    L.D = __ldg(a.dat + p);
+    const int j1 = __ldg(a.nb + a.npos + p), j3 = __ldg(a.nb + 3 * a.npos + p), j5 = __ldg(a.nb + 5 * a.npos + p);
     L.gp10 = L.gq10 = L.gq13 = L.gq14 = 0.f;
     L.gp31 = L.gq31 = L.gq33 = L.gq35 = 0.f;
     L.gp52 = L.gq52 = L.gq54 = L.gq55 = 0.f;
@@ -553,9 +528,9 @@ __device__ __forceinline__ void primal_finish(const IterArgs& a, int p, const Pr
     const float vxn = fadd(U.y, fmul(0.25f, fadd(p0, dqx)));
     const float vyn = fadd(U.z, fmul(0.25f, fadd(p1, dqy)));
     const float vzn = fadd(U.w, fmul(0.25f, fadd(p2, dqz)));
-    put4(a.bar + p, make_float4(fsub(fmul(2.0f, un), U.x), fsub(fmul(2.0f, vxn), U.y),
-                                fsub(fmul(2.0f, vyn), U.z), fsub(fmul(2.0f, vzn), U.w)), a.hint);
-    put4(a.uv + p, make_float4(un, vxn, vyn, vzn), a.hint);
+    a.bar[p] = make_float4(fsub(fmul(2.0f, un), U.x), fsub(fmul(2.0f, vxn), U.y), fsub(fmul(2.0f, vyn), U.z),
+                           fsub(fmul(2.0f, vzn), U.w));
+    a.uv[p] = make_float4(un, vxn, vyn, vzn);
     if (RES) {
         const double d0 = (double)un - U.x, d1 = (double)vxn - U.y, d2 = (double)vyn - U.z, d3 = (double)vzn - U.w;
         dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
@@ -1343,17 +1318,12 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 //   in-memory and streaming semantics (OC semantics run cfg 14 instead).
 // cfg 19: as 18 with the tiles' contiguous streams staged by TMA bulk copies
 //   (k_fused_tma).
-// cfg 20 / 21: as cfg 14 with the cube's own records loaded evict-first
-//   (ld.global.cs), and with 21 also stored evict-first (st.global.cs): in
-//   band order the cubes that gather a record come before its owner, so the
-//   owner's access is the record's last in the sweep.
 static constexpr int TUNE_SEG = 16;
 static constexpr int N_PERSIST_CFG = 6;
 static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
 static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13, CFG_BAND = 14, CFG_BAND_SWAP = 15;
 static constexpr int CFG_BAND_ILP = 16, CFG_BAND_SWAP_ILP = 17, CFG_FUSED = 18, CFG_FUSED_TMA = 19;
-static constexpr int CFG_BAND_HINT = 20, CFG_BAND_HINT_ST = 21;
 static inline bool fused_cfg(int cfg) { return cfg == CFG_FUSED || cfg == CFG_FUSED_TMA; }
 
 // Host-side tables of the fused schedule for one level: the second (ping-pong)
@@ -1364,8 +1334,7 @@ struct FuseSet {
     int ntiles;
 };
 static inline bool per_launch_cfg(int cfg) {
-    return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF || (cfg >= CFG_SWAP && cfg <= CFG_BAND_SWAP_ILP) ||
-           cfg == CFG_BAND_HINT || cfg == CFG_BAND_HINT_ST;
+    return cfg == 0 || cfg == CFG_LEAN || cfg == CFG_PF || cfg == CFG_LEAN_PF || (cfg >= CFG_SWAP && cfg <= CFG_BAND_SWAP_ILP);
 }
 static constexpr int CFG_CLUSTER8 = 10, CFG_CLUSTER16 = 11;
 static constexpr int CLUSTER_MAX_N = 1 << 17;  // cluster schedules are candidates up to this unit size
@@ -1515,8 +1484,7 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
         const bool lean = cfg == CFG_LEAN || cfg == CFG_LEAN_PF;
         a.pf = (cfg == CFG_PF || cfg == CFG_LEAN_PF || cfg == CFG_SWAP_PF) ? 1 : 0;
         a.swap = (cfg == CFG_SWAP || cfg == CFG_SWAP_PF || cfg == CFG_BAND_SWAP || cfg == CFG_BAND_SWAP_ILP) ? 1 : 0;
-        a.band = ((cfg >= CFG_BAND && cfg <= CFG_BAND_SWAP_ILP) || cfg == CFG_BAND_HINT || cfg == CFG_BAND_HINT_ST) ? 1 : 0;
-        a.hint = cfg == CFG_BAND_HINT ? 1 : (cfg == CFG_BAND_HINT_ST ? 2 : 0);
+        a.band = (cfg >= CFG_BAND && cfg <= CFG_BAND_SWAP_ILP) ? 1 : 0;
         const bool ilp2 = cfg == CFG_BAND_ILP || cfg == CFG_BAND_SWAP_ILP;
         int rc = iter_occupancy<MODE>(ctx);
         if (rc) return rc;
@@ -1590,7 +1558,7 @@ static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& ca
     int cmax = 0, rc = coop_capacity<MODE>(ctx, stop, &cmax);
     if (rc) return rc;
     cands = {0, CFG_LEAN, CFG_PF, CFG_LEAN_PF, CFG_SWAP, CFG_SWAP_PF, CFG_BAND, CFG_BAND_SWAP, CFG_BAND_ILP,
-             CFG_BAND_SWAP_ILP, CFG_BAND_HINT, CFG_BAND_HINT_ST};
+             CFG_BAND_SWAP_ILP};
     int last_grid = -1;
     if (n <= (1 << 22))
         for (int k = 1; k <= N_PERSIST_CFG; ++k) {
