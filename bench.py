@@ -442,8 +442,8 @@ def run_ours(args):
     # ---- roofline of the dominant iteration kernel (per launch, CUDA events)
     hbm, peak_kind = peaks()
     dual_ms, primal_ms = kt_d / max(1, kt_n), kt_p / max(1, kt_n)
-    if last_st.get("kt_fused"):  # one fused launch per iteration (its time is in kt_dual_ms)
-        dom, ms, bpc = "k_fused", dual_ms, BYTES_ITER
+    if last_st.get("kt_fused"):  # one fused or wavefront launch per iteration (its time is in kt_dual_ms)
+        dom, ms, bpc = ("k_wave" if last_st["kt_fused"] == 2 else "k_fused"), dual_ms, BYTES_ITER
     else:
         dom, ms, bpc = ("k_dual", dual_ms, BYTES_DUAL) if kt_d >= kt_p else ("k_primal", primal_ms, BYTES_PRIMAL)
     achieved = bpc * kt_active / (ms * 1e-3) / 1e9 if ms > 0 else None
@@ -454,7 +454,7 @@ def run_ours(args):
             "bytes_per_launch": bpc * kt_active, "avg_launch_ms": ms, "active_cubes": kt_active,
             "iteration_achieved": BYTES_ITER * kt_active / ((dual_ms + primal_ms) * 1e-3) / 1e9
             if dual_ms + primal_ms > 0 else None,
-            "other_kernel_ms": 0.0 if dom == "k_fused" else (primal_ms if dom == "k_dual" else dual_ms)}
+            "other_kernel_ms": 0.0 if dom in ("k_fused", "k_wave") else (primal_ms if dom == "k_dual" else dual_ms)}
 
     result = None
     if rank == 0:

@@ -124,8 +124,9 @@ typedef struct tgvg_stats {
     double kt_dual_ms, kt_primal_ms;
     double level_ms[TGVG_MAX_LEVELS];    /* device time of level slot k (init + iterations) */
     int32_t schedule[TGVG_MAX_LEVELS];   /* iteration schedule used for level slot k       */
-    int32_t kt_fused;                    /* 1: the timed level ran the fused kernel (kt_dual_ms
-                                            holds its time, kt_primal_ms 0)                  */
+    int32_t kt_fused;                    /* 1: the timed level ran the fused kernel, 2: the
+                                            wavefront kernel (kt_dual_ms holds its time,
+                                            kt_primal_ms 0)                                   */
     int32_t reserved;
 } tgvg_stats;
 
@@ -163,8 +164,14 @@ int tgvg_set_timing(tgvg_ctx* ctx, int on);
  * the whole level together (band order), 16 / 17 = as 14 / 15 with two cubes
  * per thread and step, 18 = one fused launch per iteration over 256-cube tiles
  * with the tile's p/q in shared memory (in-memory and streaming semantics; OC
- * runs 14), 19 = as 18 with the tiles' streams staged by TMA bulk copies, -1 =
- * let the online autotuner choose (default).  Results do not depend on it. */
+ * runs 14), 19 = as 18 with the tiles' streams staged by TMA bulk copies,
+ * 20 / 21 = one ordered-wavefront launch per iteration, each block running the
+ * dual then the primal step of a 512-cube tile once the tiles it depends on
+ * have run their dual step, with loads through L2 only (20) or through L1 too
+ * (21) (in-memory and streaming semantics on levels whose dependencies all
+ * point to earlier tiles once short runs of tiles are grouped, which holds for
+ * Morton-sorted cubes; otherwise 14; never chosen by the autotuner), -1 = let
+ * the online autotuner choose (default).  Results do not depend on it. */
 int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
 /* CUDA graphs for the level loop (1 = on, the default; 0 = off).  When every
  * level's schedule is already fixed (chosen by the autotuner in an earlier

@@ -187,10 +187,11 @@ def test_tgv_autotuned_schedules_are_exact(oracle_lib):
 
 @pytest.mark.parametrize("mode", ["inmem", "oc", "stream"])
 def test_tgv_every_schedule_is_exact(oracle_lib, mode):
-    """Each of the twenty iteration schedules (per-sweep launches with and
+    """Each of the twenty-two iteration schedules (per-sweep launches with and
     without register cap / L2 prefetch / swapped sweep directions / band order /
-    two cubes per thread, the fused tile kernel plain and TMA-staged (band order
-    in OC semantics),
+    two cubes per thread, the fused tile kernel plain and TMA-staged, the ordered
+    wavefront through L2 and through L1 (the last four run band order in OC
+    semantics),
     six persistent grid sizes, clusters of 8 and 16 CTAs), forced for every level,
     with and without the stopping test, gives the oracle's state bit for bit."""
     ctx = api.context()
@@ -202,10 +203,10 @@ def test_tgv_every_schedule_is_exact(oracle_lib, mode):
     stop, rst = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 300, tol=1e-3, check_every=10,
                                      nthreads=8)
     try:
-        for cfg in range(20):
+        for cfg in range(22):
             ctx.set_schedule(mode, -1, cfg)
             out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=40))
-            assert set(st["schedule"]) == {14 if (cfg >= 18 and mode == "oc") else cfg}
+            assert set(st["schedule"]) == {14 if (cfg >= 18 and mode == "oc") else cfg}, (cfg, mode)
             assert_state_equal(out, fixed, f"schedule {cfg} {mode}")
             out, st = api.tgv_solve(cubes, hists, leaves, mode,
                                     api.TGVParams(alpha0=2.0, alpha1=1.0, iters=300, tol=1e-3, check_every=10))
@@ -271,6 +272,41 @@ def test_tgv_unsorted_inmem_and_leaf_gaps(oracle_lib):
         ref, _ = oracle_lib.tgv_solve(cubes, h, leaves, mode, 0.5, 0.5, 15)
         out, _ = api.tgv_solve(cubes, h, leaves, mode, api.TGVParams(0.5, 0.5, 15))
         assert_state_equal(out, ref, f"gaps {mode}")
+
+
+def test_wavefront_schedules_at_scale():
+    """The ordered-wavefront schedules (20: loads through L2, 21: through L1 as
+    well) against band order (14, itself exact against the oracle) on a
+    ray-cast torus workload of about 270 k cubes, where thousands of tiles and
+    hundreds of blocks run concurrently: bit for bit in in-memory and streaming
+    semantics, with and without the stopping test.  An unsorted cube order
+    (dependencies pointing forwards) makes them fall back to band order."""
+    from tgvreconclaude_gb300 import workloads as W
+    ctx = api.context()
+    w = W.build("torus16", seed=3)
+    leaves = W.chunk_leaves(w.cubes, 8, np.random.default_rng(0))
+    try:
+        for mode, lv in (("inmem", None), ("stream", leaves)):
+            for prm in (api.TGVParams(alpha0=2.0, alpha1=1.0, iters=30),
+                        api.TGVParams(alpha0=2.0, alpha1=1.0, iters=200, tol=1e-3, check_every=10)):
+                ctx.set_schedule(mode, -1, 14)
+                ref, rst = api.tgv_solve(w.cubes, w.hists, lv, mode, prm)
+                for cfg in (20, 21):
+                    ctx.set_schedule(mode, -1, cfg)
+                    out, st = api.tgv_solve(w.cubes, w.hists, lv, mode, prm)
+                    assert set(st["schedule"]) == {cfg}
+                    assert_state_equal(out, ref, f"wavefront {cfg} {mode} tol={prm.tol}")
+                    assert st["iters_run"] == rst["iters_run"]
+        perm = np.random.default_rng(1).permutation(len(w.cubes))
+        ctx.set_schedule("inmem", -1, 20)
+        out, st = api.tgv_solve(w.cubes[perm], w.hists[perm], None, "inmem", api.TGVParams(2.0, 1.0, 10))
+        assert 14 in st["schedule"]
+        ctx.set_schedule("inmem", -1, 14)
+        ref, _ = api.tgv_solve(w.cubes[perm], w.hists[perm], None, "inmem", api.TGVParams(2.0, 1.0, 10))
+        assert_state_equal(out, ref, "unsorted fallback")
+    finally:
+        for mode in ("inmem", "oc", "stream"):
+            ctx.set_schedule(mode, -1, -1)
 
 
 def test_tgv_stopping_rule(oracle_lib):

@@ -160,6 +160,9 @@ enum BufId {
     // Stage 1
     B_P_DEP, B_P_KEY, B_P_RC, B_P_DPT, B_P_KEEP, B_P_POS, B_P_THR, B_P_CKEY, B_P_CIDX, B_P_SKEY, B_P_SIDX,
     B_P_OUT, B_P_TMP,
+    // ordered-wavefront schedule tables
+    B_W_KEYS, B_W_SKEYS, B_W_KEEP, B_W_POS, B_W_UKEYS, B_W_DEP, B_W_DOFF, B_W_FLAG, B_W_CNT, B_W_TMP, B_W_TMP2,
+    B_W_GSTART,
     B_COUNT
 };
 
@@ -183,6 +186,8 @@ struct tgvg_ctx {
     int iter_occ_ilp2[3][2] = {};      // blocks/SM of the two-cubes-per-thread sweep kernels [mode][dual, primal]
     int fused_occ[3][2] = {};          // blocks/SM of the fused iteration kernels per mode [plain, TMA-staged]
     const void* fuse_cur = nullptr;    // the fused-schedule tables of the level being run (tgv.cu), or null
+    const void* wave_cur = nullptr;    // the wavefront-schedule tables of the level being run (tgv.cu), or null
+    int wave_occ[3][2] = {};           // blocks/SM of the wavefront kernel per mode [L2 loads, L1 loads]
     cudaEvent_t lev_ev[2 * TGVG_MAX_LEVELS] = {};  // per-level start/end
     bool graphs = true;                // capture the level loop into a CUDA graph when possible
     std::vector<uint64_t> graph_key;   // problem signature of the cached graph

@@ -30,6 +30,7 @@
 #include <cstring>
 #include <vector>
 
+#include <cub/device/device_radix_sort.cuh>
 #include <nvtx3/nvToolsExt.h>
 
 #include "common.cuh"
@@ -473,17 +474,27 @@ struct PrimalLd {
     float4 U, P, Q;
     float q5;
     float2 D;
+    int j1, j3, j5;
     float gp10, gq10, gq13, gq14, gp31, gq31, gq33, gq35, gp52, gq52, gq54, gq55;
 };
 
+// The cube's own records and neighbour indices ...
 template <int MODE, bool CG>
-__device__ __forceinline__ void primal_load(const IterArgs& a, int p, PrimalLd& L) {
+__device__ __forceinline__ void primal_load_own(const IterArgs& a, int p, PrimalLd& L) {
     L.U = ld4<CG>(a.uv + p);
     L.P = ld4<CG>(a.P4 + p);
     L.Q = ld4<CG>(a.Q4 + p);
     L.q5 = ld1<CG>(a.Q1 + p);
     L.D = __ldg(a.dat + p);
-    const int j1 = __ldg(a.nb + a.npos + p), j3 = __ldg(a.nb + 3 * a.npos + p), j5 = __ldg(a.nb + 5 * a.npos + p);
+    L.j1 = __ldg(a.nb + a.npos + p);
+    L.j3 = __ldg(a.nb + 3 * a.npos + p);
+    L.j5 = __ldg(a.nb + 5 * a.npos + p);
+}
+
+// ... and the p/q of its -x/-y/-z neighbours.
+template <int MODE, bool CG>
+__device__ __forceinline__ void primal_load_gather(const IterArgs& a, PrimalLd& L) {
+    const int j1 = L.j1, j3 = L.j3, j5 = L.j5;
     L.gp10 = L.gq10 = L.gq13 = L.gq14 = 0.f;
     L.gp31 = L.gq31 = L.gq33 = L.gq35 = 0.f;
     L.gp52 = L.gq52 = L.gq54 = L.gq55 = 0.f;
@@ -502,6 +513,12 @@ __device__ __forceinline__ void primal_load(const IterArgs& a, int p, PrimalLd& 
         const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
         L.gp52 = a4.z; L.gq52 = b4.y; L.gq54 = b4.w; L.gq55 = ld1<CG>(a.Q1 + j);
     }
+}
+
+template <int MODE, bool CG>
+__device__ __forceinline__ void primal_load(const IterArgs& a, int p, PrimalLd& L) {
+    primal_load_own<MODE, CG>(a, p, L);
+    primal_load_gather<MODE, CG>(a, L);
 }
 
 template <bool RES>
@@ -1233,6 +1250,188 @@ __global__ void k_fuse_settle(int o, int n, int it0, int count, int slot0, const
     Q1[p] = Q1B[p];
 }
 
+// ---- ordered wavefront: one launch per iteration, dual then primal per tile --
+// The level is cut into tiles of 512 positions (two cubes, one after the other,
+// per thread of a 256-thread block), aligned to multiples of 32 positions so that no 128-byte
+// line of any per-cube array is shared by two tiles.  Tile c depends on tile d
+// when a cube of c has an active -x/-y/-z neighbour in d (c's primal step reads
+// its p/q), or a cube of d has an active +x/+y/+z neighbour in c (d's dual step
+// reads the bar that c's primal step overwrites).  In Morton order d < c for
+// nearly every pair; the exceptions come from the parent-code lookup, which
+// can land on the octant-0 cube of the parent a few positions back.
+// Consecutive tiles are therefore joined into groups so that every dependency
+// points to an earlier group or into its own.  Blocks claim groups in
+// increasing order from a counter; for its group a block runs the dual steps
+// of all its tiles, publishes their flags (the iteration's epoch), waits for
+// the flags of the tiles the group's primal steps depend on, and runs the
+// primal steps.  A block only ever waits for tiles of groups claimed before
+// its own (or its own, already published), whose dual steps never wait: the
+// wavefront cannot deadlock.  The waits are bounded anyway.
+// Every cube gets exactly the split schedule's arithmetic, so the results are
+// the same bit for bit; the pass reads and writes each record once per
+// iteration instead of twice.
+static constexpr int WAVE_BLOCK = 256;            // threads per block
+static constexpr int WT = 2 * WAVE_BLOCK;          // cubes per tile: two per thread
+
+struct WaveArgs {
+    const int* doff;   // [ntiles + 1] offsets into dep
+    const int* dep;    // tiles each tile's primal step waits for
+    const int* gstart; // [ngroups + 1] first tile of each group
+    int* flag;         // [ntiles] epoch of the last published dual step
+    int* claim;        // [2] group counters of alternate iterations
+    int ngroups, base, epoch;
+};
+
+__device__ __forceinline__ int wave_tile_of(int p, int base) { return (p - base) / WT; }
+
+// Dependency pairs (consumer tile << 32 | producer tile) of one level, or only
+// their count (out == nullptr); reach[c] = the last tile after c that c depends
+// on (when out == nullptr).
+template <int MODE>
+__global__ void k_wave_pairs(int o, int cnt, int base, int npos, const int* __restrict__ nb,
+                             unsigned long long* __restrict__ out, int* __restrict__ count, int* __restrict__ reach) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long key[6];
+    int k = 0;
+    if (i < cnt) {
+        const int p = o + i, tp = wave_tile_of(p, base);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            int j = __ldg(nb + (size_t)f * npos + p);
+            if (j < 0 || (MODE == M_STREAM && (j & BORDER))) continue;
+            j &= POS_MASK;
+            if (j < o || j >= o + cnt) continue;  // not active on this level
+            const int tj = wave_tile_of(j, base);
+            const int cons = (f & 1) ? tp : tj, prod = (f & 1) ? tj : tp;
+            if (cons == prod) continue;
+            if (prod > cons && !out) atomicMax(reach + cons, prod);
+            key[k++] = ((unsigned long long)cons << 32) | (unsigned)prod;
+        }
+    }
+    // warp-aggregated reservation of the output slots
+    const int lane = threadIdx.x & 31;
+    int incl = k;
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    int base_slot = 0;
+    if (lane == 31) base_slot = atomicAdd(count, incl);
+    base_slot = __shfl_sync(0xffffffffu, base_slot, 31);
+    if (out)
+        for (int m = 0; m < k; ++m) out[base_slot + incl - k + m] = key[m];
+}
+
+__global__ void k_wave_unique(int m, const unsigned long long* __restrict__ keys, int* __restrict__ keep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) keep[i] = i == 0 || keys[i] != keys[i - 1];
+}
+
+__global__ void k_wave_compact(int m, const unsigned long long* __restrict__ keys, const int* __restrict__ keep,
+                               const int* __restrict__ pos, unsigned long long* __restrict__ ukeys,
+                               int* __restrict__ dep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m && keep[i]) {
+        ukeys[pos[i]] = keys[i];
+        dep[pos[i]] = (int)(keys[i] & 0xffffffffu);
+    }
+}
+
+// doff[t] = first unique pair whose consumer is >= t (binary search).
+__global__ void k_wave_offsets(int ntiles, int nu, const unsigned long long* __restrict__ ukeys, int* __restrict__ doff) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > ntiles) return;
+    const unsigned long long want = (unsigned long long)t << 32;
+    int lo = 0, hi = nu;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ukeys[mid] < want) lo = mid + 1; else hi = mid;
+    }
+    doff[t] = lo;
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Position of cube u (0 or 1) of this thread in tile t, whether it is active
+// (in the unit and, when streaming with stopping tests, its slot still
+// running), and its stopping slot.
+template <int MODE, bool STOP>
+__device__ __forceinline__ int wave_cube(const IterArgs& a, const WaveArgs& w, int t, int u, bool& work, int& slot) {
+    const int p = w.base + t * WT + u * WAVE_BLOCK + (int)threadIdx.x;
+    work = p >= a.o && p < a.o + a.n;
+    slot = -1;
+    if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
+    if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
+    return p;
+}
+
+template <int MODE, bool RES, bool STOP, bool CG>
+__global__ void __launch_bounds__(WAVE_BLOCK, 5) k_wave(IterArgs a, WaveArgs w) {
+    __shared__ int s_group;
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.claim[(w.epoch + 1) & 1] = 0;  // the next iteration's counter
+    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
+    const int lane = threadIdx.x & 31;
+    WarpAcc wd, wp;
+    for (;;) {
+        if (threadIdx.x == 0) s_group = atomicAdd(w.claim + (w.epoch & 1), 1);
+        __syncthreads();
+        const int g = s_group;
+        if (g >= w.ngroups) break;
+        const int t0 = __ldg(w.gstart + g), t1 = __ldg(w.gstart + g + 1);
+        for (int t = t0; t < t1; ++t)
+#pragma unroll 1
+            for (int u = 0; u < 2; ++u) {
+                bool wk;
+                int sl;
+                const int p = wave_cube<MODE, STOP>(a, w, t, u, wk, sl);
+                double dd = 0.0, nd = 0.0;
+                if (wk) dual_cube<MODE, RES, CG>(a, p, dd, nd);
+                if (RES) wd.add(wk ? sl : -1, dd, nd, a.acc, 1, lane);
+            }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            for (int t = t0; t < t1; ++t) st_release(w.flag + t, w.epoch);
+        }
+        // wait for the tiles the group's primal steps read from or overwrite for
+        bool ok = true;
+        for (int t = t0; t < t1 && ok; ++t)
+            for (int k = __ldg(w.doff + t) + (int)threadIdx.x; k < __ldg(w.doff + t + 1) && ok; k += WAVE_BLOCK) {
+                const int* f = w.flag + __ldg(w.dep + k);
+                for (int spin = 0; ld_acquire(f) != w.epoch; ++spin) {
+                    if (spin > (1 << 20)) { ok = false; break; }  // about 0.1 s and more: give up, report
+                    __nanosleep(32);
+                }
+            }
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) atomicOr(a.err, 8);
+            break;
+        }
+        for (int t = t0; t < t1; ++t)
+#pragma unroll 1
+            for (int u = 0; u < 2; ++u) {
+                bool wk;
+                int sl;
+                const int p = wave_cube<MODE, STOP>(a, w, t, u, wk, sl);
+                double dd = 0.0, nd = 0.0;
+                if (wk) primal_cube<MODE, RES, CG>(a, p, dd, nd);
+                if (RES) wp.add(wk ? sl : -1, dd, nd, a.acc, 0, lane);
+            }
+        __syncthreads();  // s_group is rewritten for the next group
+    }
+    if (RES) {
+        wd.flush(a.acc, 1, lane);
+        wp.flush(a.acc, 0, lane);
+    }
+}
+
 __global__ void k_unpermute(int n, const int* __restrict__ inv, const float4* __restrict__ uv,
                             const float4* __restrict__ P4, const float4* __restrict__ Q4,
                             const float* __restrict__ Q1, float* __restrict__ out) {
@@ -1318,13 +1517,34 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 //   in-memory and streaming semantics (OC semantics run cfg 14 instead).
 // cfg 19: as 18 with the tiles' contiguous streams staged by TMA bulk copies
 //   (k_fused_tma).
+// cfg 20 / 21: one ordered-wavefront launch per iteration (k_wave): each
+//   block runs the dual then the primal step of a group of 512-cube tiles,
+//   after the tiles the primal step depends on have published their dual
+//   step; 20 reads through L2 only (ld.global.cg), 21 through L1 as well.
+//   In-memory and streaming semantics, on levels whose forward dependencies
+//   fit in small tile groups (OC semantics and other levels run 14).  Set by
+//   tgvg_set_schedule only: the autotuner does not try them, as on GB300 the
+//   tile hand-offs cost more than the traffic they save (largest three64
+//   level: 152 us per iteration against 119 us for schedule 14).
 static constexpr int TUNE_SEG = 16;
 static constexpr int N_PERSIST_CFG = 6;
 static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
 static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13, CFG_BAND = 14, CFG_BAND_SWAP = 15;
 static constexpr int CFG_BAND_ILP = 16, CFG_BAND_SWAP_ILP = 17, CFG_FUSED = 18, CFG_FUSED_TMA = 19;
+static constexpr int CFG_WAVE = 20, CFG_WAVE_L1 = 21;
 static inline bool fused_cfg(int cfg) { return cfg == CFG_FUSED || cfg == CFG_FUSED_TMA; }
+static inline bool wave_cfg(int cfg) { return cfg == CFG_WAVE || cfg == CFG_WAVE_L1; }
+
+// Host-side tables of the wavefront schedule for one level (ok: the groups
+// that make every dependency point backwards are small, so the schedule is
+// usable).
+struct WaveSet {
+    const int* doff; const int* dep; const int* gstart; int* flag; int* claim;
+    int ntiles, ngroups, base;
+    bool ok;
+};
+static constexpr int WAVE_MAX_GROUP = 8;  // tiles; larger groups leave too few blocks busy
 
 // Host-side tables of the fused schedule for one level: the second (ping-pong)
 // set of bars and p/q, the neighbour slots, the tiles' halos.
@@ -1428,11 +1648,80 @@ static int fused_occupancy(tgvg_ctx* ctx, bool tma, int* out) {
     return TGVG_OK;
 }
 
+// The schedule a unit really runs: the fused and wavefront schedules need their
+// tables (in-memory and streaming semantics; for the wavefront, a level whose
+// dependencies all point backwards), else band order.
+template <int MODE>
+static int effective_cfg(const tgvg_ctx* ctx, int cfg) {
+    const WaveSet* wz = static_cast<const WaveSet*>(ctx->wave_cur);
+    if (fused_cfg(cfg) && (MODE == M_OC || !ctx->fuse_cur)) return CFG_BAND;
+    if (wave_cfg(cfg) && (MODE == M_OC || !wz || !wz->ok)) return CFG_BAND;
+    return cfg;
+}
+
+// Blocks per SM of the wavefront kernel.
+template <int MODE>
+static int wave_occupancy(tgvg_ctx* ctx, bool l1, int* out) {
+    int& o = ctx->wave_occ[MODE][l1 ? 1 : 0];
+    if (o <= 0) {
+        int v = 0;
+        // the smallest over the variants (blocks claim work, so any grid is safe;
+        // this one fills the GPU once)
+        int u = 0;
+        cudaError_t e = l1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_wave<MODE, true, true, false>, WAVE_BLOCK, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_wave<MODE, true, true, true>, WAVE_BLOCK, 0);
+        if (e == cudaSuccess)
+            e = l1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&u, k_wave<MODE, false, false, false>, WAVE_BLOCK, 0)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&u, k_wave<MODE, false, false, true>, WAVE_BLOCK, 0);
+        v = std::min(v, u);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy query");
+        o = std::max(1, v);
+    }
+    *out = o;
+    return TGVG_OK;
+}
+
 template <int MODE>
 static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, bool stop, bool timed) {
     if (count <= 0) return TGVG_OK;
     const FuseSet* fz = static_cast<const FuseSet*>(ctx->fuse_cur);
-    if (fused_cfg(cfg) && (MODE == M_OC || !fz)) cfg = CFG_BAND;
+    const WaveSet* wz = static_cast<const WaveSet*>(ctx->wave_cur);
+    cfg = effective_cfg<MODE>(ctx, cfg);
+    if (wave_cfg(cfg)) {
+        const bool l1 = cfg == CFG_WAVE_L1;
+        int occ = 0, rc = wave_occupancy<MODE>(ctx, l1, &occ);
+        if (rc) return rc;
+        const unsigned grid = (unsigned)std::max(1, std::min(wz->ngroups, occ * ctx->sm_count));
+        // fresh flags and counters for this run of consecutive epochs
+        TGVG_CK(ctx, cudaMemsetAsync(wz->flag, 0, 4ull * std::max(1, wz->ntiles), ctx->stream));
+        TGVG_CK(ctx, cudaMemsetAsync(wz->claim, 0, 8, ctx->stream));
+        for (int it = it0; it < it0 + count; ++it) {
+            const bool res = stop && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
+            WaveArgs w{wz->doff, wz->dep, wz->gstart, wz->flag, wz->claim, wz->ngroups, wz->base, it - it0 + 1};
+            const bool mark = timed && it % TIMING_STRIDE == 0;
+            cudaEvent_t* te = mark ? &ctx->tev[3 * (it / TIMING_STRIDE)] : nullptr;
+            if (mark) TGVG_CK(ctx, record_event(te[0], ctx->stream, ctx->capturing));
+#define TGVG_WAVE(CGV)                                                                                  \
+    if (res && stop) k_wave<MODE, true, true, CGV><<<grid, WAVE_BLOCK, 0, ctx->stream>>>(a, w);         \
+    else if (res) k_wave<MODE, true, false, CGV><<<grid, WAVE_BLOCK, 0, ctx->stream>>>(a, w);           \
+    else if (stop) k_wave<MODE, false, true, CGV><<<grid, WAVE_BLOCK, 0, ctx->stream>>>(a, w);          \
+    else k_wave<MODE, false, false, CGV><<<grid, WAVE_BLOCK, 0, ctx->stream>>>(a, w);
+            if (l1) { TGVG_WAVE(false) } else { TGVG_WAVE(true) }
+#undef TGVG_WAVE
+            TGVG_LAUNCHED(ctx);
+            if (mark) {
+                TGVG_CK(ctx, record_event(te[1], ctx->stream, ctx->capturing));
+                TGVG_CK(ctx, record_event(te[2], ctx->stream, ctx->capturing));
+            }
+            if (res) {
+                const int ns = unit_slots<MODE>(a.nslot);
+                k_check<<<blocks_for(ns, 128), 128, 0, ctx->stream>>>(a.slot0, ns, a.acc, a.done, a.tol, it,
+                                                                          a.iters_run, a.resid);
+                TGVG_LAUNCHED(ctx);
+            }
+        }
+        return TGVG_OK;
+    }
     if (fused_cfg(cfg)) {
         const bool tma = cfg == CFG_FUSED_TMA;
         int occ = 0, rc = fused_occupancy<MODE>(ctx, tma, &occ);
@@ -1593,10 +1882,15 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
     if (rc) return rc;
     const int tuned = ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, n))];
     if (timed) {  // per-launch event timing needs one of the per-sweep-launch or fused schedules
-        *cfg = (per_launch_cfg(tuned) || (fused_cfg(tuned) && MODE != M_OC)) ? tuned : CFG_BAND;
+        *cfg = (per_launch_cfg(tuned) || ((fused_cfg(tuned) || wave_cfg(tuned)) && MODE != M_OC)) ? tuned : CFG_BAND;
         if (fused_cfg(*cfg)) {
             int occ = 0;
             return fused_occupancy<MODE>(ctx, *cfg == CFG_FUSED_TMA, &occ);
+        }
+        *cfg = effective_cfg<MODE>(ctx, *cfg);
+        if (wave_cfg(*cfg)) {
+            int occ = 0;
+            return wave_occupancy<MODE>(ctx, *cfg == CFG_WAVE_L1, &occ);
         }
         return TGVG_OK;
     }
@@ -1610,6 +1904,11 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
             if (MODE == M_OC) *cfg = CFG_BAND;
             int occ = 0;
             return fused_occupancy<MODE>(ctx, tuned == CFG_FUSED_TMA, &occ);
+        }
+        if (wave_cfg(tuned)) {
+            *cfg = effective_cfg<MODE>(ctx, tuned);
+            int occ = 0;
+            return wave_cfg(*cfg) ? wave_occupancy<MODE>(ctx, tuned == CFG_WAVE_L1, &occ) : TGVG_OK;
         }
         return TGVG_OK;
     }
@@ -1642,7 +1941,7 @@ static int run_unit_t(tgvg_ctx* ctx, IterArgs& a, int iters, bool stop, bool tim
         ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, a.n))] = best;
         cfg = best;
     }
-    *used = cfg;
+    *used = effective_cfg<MODE>(ctx, cfg);
     return run_segment<MODE>(ctx, a, cfg, it, iters - it, stop, timed);
 }
 
@@ -1661,6 +1960,125 @@ static int run_unit(tgvg_ctx* ctx, int mode, IterArgs& a, int iters, bool stop, 
 __global__ void k_fill_i32(int n, int* __restrict__ p, int v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = v;
+}
+
+// Wavefront tables of every level of a solve: per level, the dependency pairs
+// of its tiles, sorted and made unique, as per-tile lists (doff / dep); the
+// groups of consecutive tiles that contain every forward dependency (gstart);
+// and whether those groups are small enough for the schedule (ok).  Levels are
+// processed one at a time on scratch sized for the largest; the lists of all
+// levels share one array.
+static int build_wave_tables(tgvg_ctx* ctx, int mode, int min_d, int max_d, const int* h_bstart,
+                             int npos, const int* nb, std::vector<WaveSet>& ws) {
+    auto B = [&](int id, size_t b) { return ctx->buf(id, b); };
+    cudaStream_t st = ctx->stream;
+    const int nl = max_d - min_d + 1;
+    int64_t tiles_total = 0;
+    int max_tiles = 1;
+    std::vector<int> base(nl), ntiles(nl);
+    std::vector<int64_t> toff(nl);
+    for (int Ld = min_d; Ld <= max_d; ++Ld) {
+        const int k = Ld - min_d, o = h_bstart[Ld], c = h_bstart[Ld + 1] - h_bstart[Ld];
+        base[k] = o & ~31;
+        ntiles[k] = c > 0 ? (o + c - base[k] + WT - 1) / WT : 0;
+        max_tiles = std::max(max_tiles, ntiles[k]);
+        toff[k] = tiles_total;
+        tiles_total += ntiles[k];
+    }
+    auto* cnt = (int*)B(B_W_CNT, 4ull * (nl + 2));
+    auto* reach = (int*)B(B_W_POS, 4ull * std::max<int64_t>(1, tiles_total));
+    if (!cnt || !reach) return TGVG_ERR_NOMEM;
+    TGVG_CK(ctx, cudaMemsetAsync(cnt, 0, 4ull * (nl + 2), st));
+    TGVG_CK(ctx, cudaMemsetAsync(reach, 0xff, 4ull * std::max<int64_t>(1, tiles_total), st));
+    for (int Ld = min_d; Ld <= max_d; ++Ld) {
+        const int k = Ld - min_d, o = h_bstart[Ld], c = h_bstart[Ld + 1] - h_bstart[Ld];
+        if (c <= 0) continue;
+        if (mode == M_INMEM)
+            k_wave_pairs<M_INMEM><<<blocks_for(c, 256), 256, 0, st>>>(o, c, base[k], npos, nb, nullptr, cnt + k,
+                                                                    reach + toff[k]);
+        else
+            k_wave_pairs<M_STREAM><<<blocks_for(c, 256), 256, 0, st>>>(o, c, base[k], npos, nb, nullptr, cnt + k,
+                                                                     reach + toff[k]);
+        TGVG_LAUNCHED(ctx);
+    }
+    std::vector<int> h_cnt(nl), h_reach(size_t(std::max<int64_t>(1, tiles_total)));
+    TGVG_CK(ctx, cudaMemcpyAsync(h_cnt.data(), cnt, 4ull * nl, cudaMemcpyDeviceToHost, st));
+    TGVG_CK(ctx, cudaMemcpyAsync(h_reach.data(), reach, 4ull * h_reach.size(), cudaMemcpyDeviceToHost, st));
+    TGVG_CK(ctx, cudaStreamSynchronize(st));
+    // groups: extend each group until no tile in it depends on a tile after it
+    std::vector<int> h_gstart;
+    std::vector<int64_t> goff(nl);
+    std::vector<int> ngroups(nl), maxg(nl, 0);
+    for (int k = 0; k < nl; ++k) {
+        goff[k] = (int64_t)h_gstart.size();
+        int t = 0;
+        while (t < ntiles[k]) {
+            const int g0 = t;
+            int end = t + 1;
+            for (; t < end; ++t) end = std::max(end, h_reach[toff[k] + t] + 1);
+            h_gstart.push_back(g0);
+            maxg[k] = std::max(maxg[k], t - g0);
+        }
+        h_gstart.push_back(ntiles[k]);
+        ngroups[k] = (int)(h_gstart.size() - goff[k]) - 1;
+    }
+    int64_t max_pairs = 1, dep_total = 1, off_total = 0;
+    for (int k = 0; k < nl; ++k) {
+        max_pairs = std::max<int64_t>(max_pairs, h_cnt[k]);
+        dep_total += h_cnt[k];
+        off_total += ntiles[k] + 1;
+    }
+    auto* keys = (unsigned long long*)B(B_W_KEYS, 8ull * max_pairs);
+    auto* skeys = (unsigned long long*)B(B_W_SKEYS, 8ull * max_pairs);
+    auto* keep = (int*)B(B_W_KEEP, 4ull * max_pairs);
+    auto* kpos = (int*)B(B_W_TMP2, 4ull * max_pairs);
+    auto* ukeys = (unsigned long long*)B(B_W_UKEYS, 8ull * max_pairs);
+    auto* dep = (int*)B(B_W_DEP, 4ull * dep_total);
+    auto* doff = (int*)B(B_W_DOFF, 4ull * std::max<int64_t>(1, off_total));
+    auto* gst = (int*)B(B_W_GSTART, 4ull * h_gstart.size());
+    auto* flag = (int*)B(B_W_FLAG, 4ull * max_tiles + 64);
+    if (!keys || !skeys || !keep || !kpos || !ukeys || !dep || !doff || !gst || !flag) return TGVG_ERR_NOMEM;
+    TGVG_CK(ctx, cudaMemcpyAsync(gst, h_gstart.data(), 4ull * h_gstart.size(), cudaMemcpyHostToDevice, st));
+    int64_t dep_at = 0, off_at = 0;
+    for (int Ld = min_d; Ld <= max_d; ++Ld) {
+        const int k = Ld - min_d, o = h_bstart[Ld], c = h_bstart[Ld + 1] - h_bstart[Ld];
+        if (c <= 0) continue;
+        WaveSet& w = ws[Ld];
+        w = WaveSet{doff + off_at, dep + dep_at, gst + goff[k], flag, flag + max_tiles, ntiles[k], ngroups[k],
+                    base[k], maxg[k] <= WAVE_MAX_GROUP};
+        const int m = h_cnt[k];
+        int nu = 0;
+        if (w.ok && m > 0) {
+            TGVG_CK(ctx, cudaMemsetAsync(cnt + nl, 0, 4, st));
+            if (mode == M_INMEM)
+                k_wave_pairs<M_INMEM><<<blocks_for(c, 256), 256, 0, st>>>(o, c, base[k], npos, nb, keys, cnt + nl,
+                                                                        nullptr);
+            else
+                k_wave_pairs<M_STREAM><<<blocks_for(c, 256), 256, 0, st>>>(o, c, base[k], npos, nb, keys, cnt + nl,
+                                                                         nullptr);
+            TGVG_LAUNCHED(ctx);
+            int bits = 1;
+            while ((1 << bits) < ntiles[k] + 1) ++bits;
+            size_t tb = 0;
+            TGVG_CK(ctx, cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, skeys, m, 0, 32 + bits, st));
+            void* tmp = B(B_W_TMP, std::max<size_t>(tb, 16));
+            if (!tmp) return TGVG_ERR_NOMEM;
+            TGVG_CK(ctx, cub::DeviceRadixSort::SortKeys(tmp, tb, keys, skeys, m, 0, 32 + bits, st));
+            k_wave_unique<<<blocks_for(m, 256), 256, 0, st>>>(m, skeys, keep);
+            TGVG_LAUNCHED(ctx);
+            int64_t nu64 = 0;
+            int rc = scan_exclusive(ctx, keep, m, kpos, &nu64);
+            if (rc) return rc;
+            nu = (int)nu64;
+            k_wave_compact<<<blocks_for(m, 256), 256, 0, st>>>(m, skeys, keep, kpos, ukeys, dep + dep_at);
+            TGVG_LAUNCHED(ctx);
+        }
+        k_wave_offsets<<<blocks_for(ntiles[k] + 1, 256), 256, 0, st>>>(ntiles[k], nu, ukeys, doff + off_at);
+        TGVG_LAUNCHED(ctx);
+        dep_at += nu;
+        off_at += ntiles[k] + 1;
+    }
+    return TGVG_OK;
 }
 
 int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists, int64_t n64,
@@ -1850,12 +2268,23 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         }
         fused_ok = true;
     }
+    // ---- wavefront-schedule tables, per level (in-memory and streaming semantics)
+    std::vector<WaveSet> wsets(NBUCKET, WaveSet{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0, false});
+    bool wave_wanted = false;  // only a schedule set by tgvg_set_schedule runs it
+    for (int c : ctx->tune[mode]) wave_wanted |= wave_cfg(c);
+    if (wave_wanted && mode != M_OC && fiters > 0 && n_act > 0) {
+        const int rc = build_wave_tables(ctx, mode, min_d, max_d, h_bstart, n, nb, wsets);
+        if (rc) return rc;
+    }
     // the level being planned or run; cleared on every return
     struct FuseCur {
         tgvg_ctx* c;
-        ~FuseCur() { c->fuse_cur = nullptr; }
+        ~FuseCur() { c->fuse_cur = nullptr; c->wave_cur = nullptr; }
     } fuse_guard{ctx};
-    auto set_fuse = [&](int Ld) { ctx->fuse_cur = fused_ok ? &fsets[Ld] : nullptr; };
+    auto set_fuse = [&](int Ld) {
+        ctx->fuse_cur = fused_ok ? &fsets[Ld] : nullptr;
+        ctx->wave_cur = wsets[Ld].doff ? &wsets[Ld] : nullptr;
+    };
     TGVG_CK(ctx, cudaEventRecord(e1, ctx->stream));
 
     // ---- levels
@@ -2063,7 +2492,10 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     int h_err = 0;
     TGVG_CK(ctx, cudaMemcpyAsync(&h_err, flags + 6, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    if (h_err) return ctx->fail(TGVG_ERR_TIMEOUT, "a grid barrier of the persistent iteration kernel timed out");
+    if (h_err)
+        return ctx->fail(TGVG_ERR_TIMEOUT, (h_err & 1) ? "a grid barrier of the persistent iteration kernel timed out"
+                                           : (h_err & 4) ? "a TMA stage wait of the fused iteration kernel timed out"
+                                                         : "a tile wait of the wavefront iteration kernel timed out");
     for (int k = 0; k < nlv; ++k) {
         const Level& lvl = levels[k];
         st.n_levels = k + 1;
@@ -2120,7 +2552,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         st.kt_depth = t_level;
         st.kt_launches = nt;
         for (int k = 0; k < nlv; ++k)
-            if (levels[k].d == t_level) st.kt_fused = fused_cfg(used[k]) ? 1 : 0;
+            if (levels[k].d == t_level) st.kt_fused = fused_cfg(used[k]) ? 1 : (wave_cfg(used[k]) ? 2 : 0);
         st.kt_active = h_bstart[t_level + 1] - h_bstart[t_level];
         st.kt_dual_ms = dsum;
         st.kt_primal_ms = psum;
