@@ -119,7 +119,7 @@ def build_cubes(dm, scene_origin, r_root) -> np.ndarray:
     s, keep = _depthmap_struct(dm)
     o = np.ascontiguousarray(scene_origin, np.float32)
     n = C.c_int64(0)
-    out = np.zeros(keep.size, F.CUBE_DTYPE)  # at most one cube per pixel
+    out = np.empty(keep.size, F.CUBE_DTYPE)  # at most one cube per pixel
     ctx.check(ctx.lib.tgvg_build_cubes(ctx.h, C.byref(s), _p(o), C.c_float(r_root), _p(out), len(out), C.byref(n)),
               "tgvg_build_cubes")
     return out[: n.value].copy()
@@ -145,7 +145,7 @@ def merge_cubes(arrays) -> np.ndarray:
     ptrs = (C.c_void_p * max(1, len(arrs)))(*[a.ctypes.data if len(a) else None for a in arrs])
     ns = np.array([len(a) for a in arrs] or [0], np.int64)
     n = C.c_int64(0)
-    out = np.zeros(int(ns.sum()), F.CUBE_DTYPE)  # the merge never grows the list
+    out = np.empty(int(ns.sum()), F.CUBE_DTYPE)  # the merge never grows the list
     ctx.check(ctx.lib.tgvg_merge_cubes(ctx.h, ptrs, _p(ns), len(arrs), _p(out), len(out), C.byref(n)),
               "tgvg_merge_cubes")
     return out[: n.value].copy()
@@ -165,10 +165,10 @@ def balance_cubes(cubes, r_root) -> np.ndarray:
     ctx = context()
     c = np.ascontiguousarray(cubes, F.CUBE_DTYPE)
     n = C.c_int64(0)
-    out = np.zeros(4 * len(c) + 4096, F.CUBE_DTYPE)
+    out = np.empty(4 * len(c) + 4096, F.CUBE_DTYPE)
     rc = ctx.lib.tgvg_balance_cubes(ctx.h, _p(c), len(c), C.c_float(r_root), _p(out), len(out), C.byref(n))
     if rc == TGVG_ERR_LIMIT:  # more bridges than the first guess: run again with the exact size
-        out = np.zeros(n.value, F.CUBE_DTYPE)
+        out = np.empty(n.value, F.CUBE_DTYPE)
         rc = ctx.lib.tgvg_balance_cubes(ctx.h, _p(c), len(c), C.c_float(r_root), _p(out), len(out), C.byref(n))
     ctx.check(rc, "tgvg_balance_cubes")
     return out[: n.value].copy()

@@ -341,10 +341,14 @@ struct Dev {
     }
 };
 
-int merge_dev(tgvg_ctx* ctx, const tgvg_cube* const* in, const int64_t* counts, int k, std::vector<tgvg_cube>& out) {
-    out.clear();
+// Results go to `vec` (resized) when given, else to `out` when it has room
+// (cap), else TGVG_ERR_LIMIT; *count receives their number.
+int merge_dev(tgvg_ctx* ctx, const tgvg_cube* const* in, const int64_t* counts, int k, std::vector<tgvg_cube>* vec,
+              tgvg_cube* out, int64_t cap, int64_t* count) {
     int64_t n = 0;
     for (int s = 0; s < k; ++s) n += counts[s];
+    *count = 0;
+    if (vec) vec->clear();
     if (n == 0) return TGVG_OK;
     if (n > (int64_t(1) << 31) - 1) return ctx->fail(TGVG_ERR_LIMIT, "more than 2^31 - 1 cubes");
     cudaStream_t st = ctx->stream;
@@ -379,8 +383,16 @@ int merge_dev(tgvg_ctx* ctx, const tgvg_cube* const* in, const int64_t* counts, 
     if (!res) return ctx->fail(TGVG_ERR_NOMEM, "merge output");
     k_merge_runs<<<grid_of(n, 256), 256, 0, st>>>(n, cat, sidx, start, pos, res);
     TGVG_LAUNCHED(ctx);
-    out.resize(size_t(runs));
-    TGVG_CK(ctx, cudaMemcpyAsync(out.data(), res, sizeof(tgvg_cube) * runs, cudaMemcpyDeviceToHost, st));
+    *count = runs;
+    if (vec) {
+        vec->resize(size_t(runs));
+        out = vec->data();
+    } else if (!out) {
+        return TGVG_OK;
+    } else if (cap < runs) {
+        return TGVG_ERR_LIMIT;
+    }
+    TGVG_CK(ctx, cudaMemcpyAsync(out, res, sizeof(tgvg_cube) * runs, cudaMemcpyDeviceToHost, st));
     TGVG_CK(ctx, cudaStreamSynchronize(st));
     return TGVG_OK;
 }
@@ -393,9 +405,11 @@ struct BalanceSets {
     KeySet dcs() const { return KeySet{dc_keys, cap - 1, DC_EMPTY}; }
 };
 
-int balance_dev(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n, float r_root, std::vector<tgvg_cube>& out,
-                int64_t* rounds_out) {
-    out.clear();
+// Results as merge_dev's.
+int balance_dev(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n, float r_root, std::vector<tgvg_cube>* vec,
+                tgvg_cube* out, int64_t cap, int64_t* count) {
+    *count = 0;
+    if (vec) vec->clear();
     if (n == 0) return TGVG_OK;
     if (n > (int64_t(1) << 30)) return ctx->fail(TGVG_ERR_LIMIT, "more than 2^30 cubes");
     cudaStream_t st = ctx->stream;
@@ -457,14 +471,13 @@ int balance_dev(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n, float r_root, 
     uint64_t wcap = 0;
     unsigned long long *wdc = nullptr, *wdc_slot = nullptr, *wcell = nullptr, *wcell_slot = nullptr;
 
-    int64_t h = 0, t = n, rounds = 0;
+    int64_t h = 0, t = n;
     while (h < t) {
         const int64_t wn = std::min<int64_t>(t - h, wmax);
         const int64_t m = 6 * wn;
         k_bal_propose<<<grid_of(m, 256), 256, 0, st>>>(h, wn, q, S.cells(), Window{S.cells(), nullptr, false}, prop,
                                                         nullptr, nullptr);
         TGVG_LAUNCHED(ctx);
-        ++rounds;
         int64_t nl = 0;
         unsigned long long limit = (unsigned long long)m;
         for (int it = 0;; ++it) {
@@ -502,7 +515,6 @@ int balance_dev(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n, float r_root, 
             k_bal_propose<<<grid_of(m, 256), 256, 0, st>>>(h, wn, q, S.cells(), Window{kwcell, wcell_slot, true},
                                                             prop2, prop, fc);
             TGVG_LAUNCHED(ctx);
-            ++rounds;
             unsigned long long first = 0;
             TGVG_CK(ctx, cudaMemcpyAsync(&first, fc, sizeof(first), cudaMemcpyDeviceToHost, st));
             TGVG_CK(ctx, cudaStreamSynchronize(st));
@@ -548,7 +560,6 @@ int balance_dev(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n, float r_root, 
         h += done;
         t += na;
     }
-    if (rounds_out) *rounds_out = rounds;
 
     // Output: averaged input keys, then the bridges, sorted by (code, depth).
     size_t tb = 0;
@@ -587,8 +598,16 @@ int balance_dev(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n, float r_root, 
     TGVG_CK(ctx, cub::DeviceRadixSort::SortPairs(tmp2, tb, okey, sokey, oidx, soidx, (int)no, 0, 64, st));
     k_bal_emit<<<grid_of(no, 256), 256, 0, st>>>(no, sokey, soidx, orc, res);
     TGVG_LAUNCHED(ctx);
-    out.resize(size_t(no));
-    TGVG_CK(ctx, cudaMemcpyAsync(out.data(), res, sizeof(tgvg_cube) * no, cudaMemcpyDeviceToHost, st));
+    *count = no;
+    if (vec) {
+        vec->resize(size_t(no));
+        out = vec->data();
+    } else if (!out) {
+        return TGVG_OK;
+    } else if (cap < no) {
+        return TGVG_ERR_LIMIT;
+    }
+    TGVG_CK(ctx, cudaMemcpyAsync(out, res, sizeof(tgvg_cube) * no, cudaMemcpyDeviceToHost, st));
     TGVG_CK(ctx, cudaStreamSynchronize(st));
     return TGVG_OK;
 }
@@ -612,17 +631,8 @@ extern "C" int tgvg_merge_cubes(tgvg_ctx* ctx, const tgvg_cube* const* arrays, c
     if (!ctx || !count || k < 0 || (k > 0 && (!arrays || !counts))) return TGVG_ERR_INVALID;
     for (int s = 0; s < k; ++s)
         if (counts[s] < 0 || (counts[s] > 0 && !arrays[s])) return TGVG_ERR_INVALID;
-    std::vector<tgvg_cube> res;
-    {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        const int rc = merge_dev(ctx, arrays, counts, k, res);
-        if (rc) return rc;
-    }
-    *count = int64_t(res.size());
-    if (!out) return TGVG_OK;
-    if (cap < int64_t(res.size())) return TGVG_ERR_LIMIT;
-    if (!res.empty()) std::memcpy(out, res.data(), sizeof(tgvg_cube) * res.size());
-    return TGVG_OK;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return merge_dev(ctx, arrays, counts, k, nullptr, out, cap, count);
 }
 
 extern "C" int tgvg_kway_merge(tgvg_ctx* ctx, const char* const* in_paths, int32_t k, const char* out_path) {
@@ -650,7 +660,8 @@ extern "C" int tgvg_kway_merge(tgvg_ctx* ctx, const char* const* in_paths, int32
     std::vector<tgvg_cube> res;
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
-        const int rc = merge_dev(ctx, ptr.data(), cnt.data(), k, res);
+        int64_t nres = 0;
+        const int rc = merge_dev(ctx, ptr.data(), cnt.data(), k, &res, nullptr, 0, &nres);
         if (rc) return rc;
     }
     const int rc = write_cube_file(out_path, r_root, res);
@@ -660,17 +671,8 @@ extern "C" int tgvg_kway_merge(tgvg_ctx* ctx, const char* const* in_paths, int32
 extern "C" int tgvg_balance_cubes(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n, float r_root, tgvg_cube* out,
                                   int64_t cap, int64_t* count) {
     if (!ctx || !count || n < 0 || (n > 0 && !cubes)) return TGVG_ERR_INVALID;
-    std::vector<tgvg_cube> res;
-    {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        const int rc = balance_dev(ctx, cubes, n, r_root, res, nullptr);
-        if (rc) return rc;
-    }
-    *count = int64_t(res.size());
-    if (!out) return TGVG_OK;
-    if (cap < int64_t(res.size())) return TGVG_ERR_LIMIT;
-    if (!res.empty()) std::memcpy(out, res.data(), sizeof(tgvg_cube) * res.size());
-    return TGVG_OK;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return balance_dev(ctx, cubes, n, r_root, nullptr, out, cap, count);
 }
 
 extern "C" int tgvg_balance_octree(tgvg_ctx* ctx, const char* in_path, const char* out_path) {
@@ -683,7 +685,8 @@ extern "C" int tgvg_balance_octree(tgvg_ctx* ctx, const char* in_path, const cha
     std::vector<tgvg_cube> res;
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
-        rc = balance_dev(ctx, cubes.data(), int64_t(cubes.size()), r_root, res, nullptr);
+        int64_t nres = 0;
+        rc = balance_dev(ctx, cubes.data(), int64_t(cubes.size()), r_root, &res, nullptr, 0, &nres);
         if (rc) return rc;
     }
     rc = write_cube_file(out_path, r_root, res);

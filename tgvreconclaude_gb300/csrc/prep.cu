@@ -162,10 +162,13 @@ static void radius_thresholds(float* t) {
     }
 }
 
+// The cubes of one map.  *count receives their number; they are copied to
+// out when it has room for them (cap), else TGVG_ERR_LIMIT; out == nullptr
+// asks for the count only.
 static int build_cubes(tgvg_ctx* ctx, const tgvg_depthmap* dm, const float* origin, float r_root,
-                       std::vector<tgvg_cube>& out) {
+                       tgvg_cube* out, int64_t cap, int64_t* count) {
     const int64_t npix = int64_t(dm->width) * dm->height;
-    out.clear();
+    *count = 0;
     if (npix <= 0) return TGVG_OK;
     if (npix > (int64_t(1) << 30)) return ctx->fail(TGVG_ERR_LIMIT, "depth map larger than 2^30 pixels");
     float thr[21];
@@ -193,7 +196,9 @@ static int build_cubes(tgvg_ctx* ctx, const tgvg_depthmap* dm, const float* orig
     int64_t nc = 0;
     int rc2 = scan_exclusive(ctx, keep, npix, pos, &nc);
     if (rc2) return rc2;
-    if (nc == 0) return TGVG_OK;
+    *count = nc;
+    if (nc == 0 || !out) return TGVG_OK;
+    if (cap < nc) return TGVG_ERR_LIMIT;
     auto* ckey = (unsigned long long*)B(B_P_CKEY, 8ull * nc);
     auto* cidx = (int*)B(B_P_CIDX, 4ull * nc);
     auto* skey = (unsigned long long*)B(B_P_SKEY, 8ull * nc);
@@ -211,8 +216,7 @@ static int build_cubes(tgvg_ctx* ctx, const tgvg_depthmap* dm, const float* orig
     TGVG_CK(ctx, cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, ckey, skey, cidx, sidx, (int)nc, 0, 63, st));
     k_stage1_emit<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>((int)nc, skey, sidx, rc, dpt, cub_out);
     TGVG_LAUNCHED(ctx);
-    out.resize(size_t(nc));
-    TGVG_CK(ctx, cudaMemcpyAsync(out.data(), cub_out, sizeof(tgvg_cube) * nc, cudaMemcpyDeviceToHost, st));
+    TGVG_CK(ctx, cudaMemcpyAsync(out, cub_out, sizeof(tgvg_cube) * nc, cudaMemcpyDeviceToHost, st));
     TGVG_CK(ctx, cudaStreamSynchronize(st));
     return TGVG_OK;
 }
@@ -226,17 +230,8 @@ extern "C" int tgvg_build_cubes(tgvg_ctx* ctx, const tgvg_depthmap* dm, const fl
     if (!ctx || !dm || !origin3 || !count || dm->width < 0 || dm->height < 0 ||
         (int64_t(dm->width) * dm->height > 0 && !dm->depths) || !std::isfinite(r_root) || !(r_root > 0.0f))
         return TGVG_ERR_INVALID;
-    std::vector<tgvg_cube> cubes;
-    {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        const int rc = build_cubes(ctx, dm, origin3, r_root, cubes);
-        if (rc) return rc;
-    }
-    *count = int64_t(cubes.size());
-    if (!out) return TGVG_OK;
-    if (cap < int64_t(cubes.size())) return TGVG_ERR_LIMIT;
-    if (!cubes.empty()) std::memcpy(out, cubes.data(), sizeof(tgvg_cube) * cubes.size());
-    return TGVG_OK;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return build_cubes(ctx, dm, origin3, r_root, out, cap, count);
 }
 
 extern "C" int tgvg_build_cubes_file(tgvg_ctx* ctx, const tgvg_depthmap* dm, const float* origin3, float r_root,
@@ -245,6 +240,7 @@ extern "C" int tgvg_build_cubes_file(tgvg_ctx* ctx, const tgvg_depthmap* dm, con
     std::vector<tgvg_cube> cubes(size_t(std::max(0, dm ? dm->width : 0)) * size_t(std::max(0, dm ? dm->height : 0)));
     int rc = tgvg_build_cubes(ctx, dm, origin3, r_root, cubes.data(), int64_t(cubes.size()), &n);
     if (rc) return rc;
+    cubes.resize(size_t(n));
     char hdr[16] = {'T', 'G', 'V', '1'};
     const uint32_t ver = 1, cnt = uint32_t(n);
     std::memcpy(hdr + 4, &ver, 4);
