@@ -261,6 +261,55 @@ def measure_e2e(args, w, ctx, prm, mode, leaves, out_t, stream):
             "d2h_bytes_per_step": int(52 * n), "steps": steps, "wall_s": t_wall, "matches_device_run": same}
 
 
+def histogram_kernel_eval(ctx, w, cubes_t, nbins, expect, stream, reps=5):
+    """The binning kernel alone (tgvg_compute_histograms_dev) on device-resident
+    pyramids and cubes, timed with CUDA events on the library's stream, with its
+    algorithmic bytes: per pair one texel (4 B), per cube its record (16 B) and
+    histogram row (4 B per bin) once."""
+    import ctypes as C
+    import torch
+    from tgvreconclaude_gb300 import _native as N, api
+    lib, cams = ctx.lib, w.cams
+    ncam, n = len(cams), len(w.cubes)
+    sizes = []
+    for c in cams:
+        dims = (C.c_int32 * 26)()
+        nl = lib.tgvg_pyramid_dims(c.width, c.height, dims)
+        sizes.append(sum(dims[2 * k] * dims[2 * k + 1] for k in range(nl)))
+    levels = [np.empty(sz, np.float32) for sz in sizes]
+    arr = (N.Camera * ncam)(*cams)
+    basep = (C.c_void_p * ncam)(*[np.ascontiguousarray(d, np.float32).ctypes.data for d in w.depths])
+    outp = (C.c_void_p * ncam)(*[lv.ctypes.data for lv in levels])
+    ctx.check(lib.tgvg_build_pyramids(ctx.h, arr, ncam, basep, outp), "tgvg_build_pyramids")
+    tex = torch.from_numpy(np.concatenate(levels)).cuda()
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    d_out = torch.empty((n, nbins), dtype=torch.int32, device="cuda")
+    o = np.asarray(w.cfg["origin"], np.float32)
+
+    def call():
+        ctx.check(lib.tgvg_compute_histograms_dev(ctx.h, cubes_t.data_ptr(), n, arr, ncam, tex.data_ptr(), api._p(off),
+                                                  api._p(o), float(w.cfg["r_root"]), nbins, d_out.data_ptr()),
+                  "tgvg_compute_histograms_dev")
+
+    call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    pairs = n * ncam
+    nbytes = 4 * pairs + n * (16 + 4 * nbins)
+    hbm, peak_kind = peaks()
+    return {"kernel": "k_histograms", "ms": ms, "pairs_per_s": pairs / (ms * 1e-3),
+            "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / (ms * 1e-3) / 1e9,
+            "frac": nbytes / (ms * 1e-3) / 1e9 / hbm, "peak_kind": peak_kind,
+            "texels_on_device_mb": 4 * int(off[-1]) / 1e6,
+            "matches_host_call": bool(np.array_equal(d_out.cpu().numpy().view(np.uint32), expect))}
+
+
 def surface_eval(args, w, out_t):
     """Surface extraction (extract_surface with has_data and normals) of the
     solved state through the host-buffer C ABI call, and the CPU oracle on a
@@ -304,7 +353,9 @@ def stages13_eval(args, w):
         rt = np.linalg.inv(np.asarray(cam.rt_inv[:], np.float64).reshape(4, 4)).astype(np.float32)
         return dict(depth=d, rt=rt, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy)
 
-    maps = [as_map(c, d) for c, d in zip(w.cams, w.depths)]
+    import torch
+    pinned = [torch.from_numpy(np.ascontiguousarray(d, np.float32)).pin_memory().numpy() for d in w.depths]
+    maps = [as_map(c, d) for c, d in zip(w.cams, pinned)]  # depth maps in pinned host memory
     api.build_cubes(maps[0], o, r)  # warm-up
     t0 = time.perf_counter()
     arrs = [api.build_cubes(m, o, r) for m in maps]
@@ -319,7 +370,8 @@ def stages13_eval(args, w):
            "ms_e2e": {"stage1": 1e3 * (t1 - t0), "merge": 1e3 * (t2 - t1), "balance": 1e3 * (t3 - t2)},
            "stage1_pixels_per_s_e2e": px / (t1 - t0), "merge_cubes_per_s_e2e": n1 / (t2 - t1),
            "balance_cubes_per_s_e2e": len(merged) / (t3 - t2),
-           "what": "build_cubes per map, merge_cubes, balance_cubes; host arrays in and out"}
+           "what": "build_cubes per map (depth maps in pinned host memory), merge_cubes, balance_cubes; "
+                   "host arrays in and out"}
     if not args.skip_cpu:
         sys.path.insert(0, os.path.join(HERE, "oracle"))
         import oracle as O
@@ -464,14 +516,20 @@ def run_ours(args):
         e2e = {} if args.skip_e2e else measure_e2e(args, w, ctx, prm, mode, leaves, out_t, stream)
 
         # ---- Stage 5 on the same workload: pyramids + binning, host buffers in/out
+        # (depth maps and cubes in pinned host memory, as for the solver's e2e)
         hs = {}
         if not args.skip_hist:
+            pin_maps = [torch.from_numpy(np.ascontiguousarray(d, np.float32)).pin_memory().numpy() for d in w.depths]
+            pin_cubes = torch.from_numpy(w.cubes.view(np.int32).reshape(n, 4).copy()).pin_memory().numpy()
+            pin_cubes = pin_cubes.view(F.CUBE_DTYPE).reshape(n)
             h_t0 = time.perf_counter()
-            hh = api.compute_histograms_from_maps(w.cubes, w.cams, w.depths, cfg["origin"], cfg["r_root"], nbins)
+            hh = api.compute_histograms_from_maps(pin_cubes, w.cams, pin_maps, cfg["origin"], cfg["r_root"], nbins)
             h_dt = time.perf_counter() - h_t0
             pairs = n * len(w.cams)
             hs = {"pairs_per_s_e2e": pairs / h_dt, "ms_e2e": 1e3 * h_dt, "pairs": pairs,
                   "matches_workload": bool(np.array_equal(hh, w.hists))}
+            if w.cams:
+                hs["device"] = histogram_kernel_eval(ctx, w, cubes_t, nbins, hh, stream)
 
         # ---- CPU oracle baseline on a bounded sample (1 thread), and the error
         # of this package's FP32 result against an FP64 run of the same solver

@@ -312,7 +312,7 @@ def compute_histograms_from_maps(cubes, cams, bases, scene_origin, r_root, nbins
     cams: sequence of N.Camera; bases: sequence of (H, W) float32 arrays."""
     ctx = context()
     cubes = np.ascontiguousarray(cubes, F.CUBE_DTYPE)
-    out = np.zeros((len(cubes), nbins), np.uint32)
+    out = np.empty((len(cubes), nbins), np.uint32)
     if len(cubes) == 0:
         return out
     bases = [np.ascontiguousarray(b, np.float32) for b in bases]
