@@ -105,19 +105,41 @@ __global__ void k_pyramid_level(const DevCam* __restrict__ cams, float* __restri
 static constexpr int HIST_BLOCK = 256;
 static constexpr int CAM_BATCH = 64;
 
-struct Thresholds { float t[13]; };
+// t[k] (k = 1..12): the smallest float x with (int)log2f(x) >= k.  expo: every
+// t[k] lies in (2^(k-1), 2^k], so for x >= 1 the level is the float exponent e
+// of x, plus one when x >= t[e+1].
+struct Thresholds {
+    float t[13];
+    int expo;
+};
 
-template <int NB>
+// Host side of the thresholds: the expo property checked on the values.
+static inline void finish_thresholds(Thresholds& thr) {
+    thr.expo = 1;
+    for (int k = 1; k < 13; ++k)
+        if (!(thr.t[k] > std::ldexp(1.0f, k - 1) && thr.t[k] <= std::ldexp(1.0f, k))) thr.expo = 0;
+}
+
+// PACK: the bin counts are kept as 16-bit fields of 64-bit words (four bins a
+// word), which holds when no cube can collect more than 65535 votes; one shift
+// and a few predicated adds per pair instead of a compare and add per bin.
+template <int NB, bool PACK>
 __global__ void __launch_bounds__(HIST_BLOCK)
 k_histograms(const uint4* __restrict__ cubes, int64_t n, const DevCam* __restrict__ cams, int ncam,
              const float* __restrict__ tex, float ox, float oy, float oz, float r_root,
              Thresholds thr, uint32_t* __restrict__ out) {
     __shared__ DevCam s_cam[CAM_BATCH];
+    __shared__ float s_thr[13];
+    if (threadIdx.x < 13) s_thr[threadIdx.x] = thr.t[threadIdx.x];
     const int64_t i = int64_t(blockIdx.x) * HIST_BLOCK + threadIdx.x;
     const bool valid = i < n;
+    constexpr int NW = (NB + 3) / 4;
     uint32_t bins[NB];
+    uint64_t pk[NW];
 #pragma unroll
     for (int k = 0; k < NB; ++k) bins[k] = 0;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) pk[k] = 0;
 
     // cube_center (histogram.cpp:118-125)
     float px = 0.f, py = 0.f, pz = 0.f, r_c = 0.f;
@@ -172,8 +194,13 @@ k_histograms(const uint4* __restrict__ cubes, int64_t n, const DevCam* __restric
             const float xm = (1.0f < fp) ? fp : 1.0f;
             int lv = 0;
             if (xm < INFINITY) {
+                if (thr.expo) {
+                    const int e = min((int)(__float_as_uint(xm) >> 23) - 127, 12);  // xm >= 1
+                    lv = e + ((e < 12 && xm >= s_thr[e + 1]) ? 1 : 0);
+                } else {
 #pragma unroll
-                for (int k = 1; k < 13; ++k) lv += (xm >= thr.t[k]) ? 1 : 0;
+                    for (int k = 1; k < 13; ++k) lv += (xm >= s_thr[k]) ? 1 : 0;
+                }
             }
             lv = min(lv, c.nlev - 1);
             const int lw = max(1, c.W >> lv), lh = max(1, c.H >> lv);
@@ -188,11 +215,21 @@ k_histograms(const uint4* __restrict__ cubes, int64_t n, const DevCam* __restric
             a = (a < -1.0f) ? -1.0f : ((1.0f < a) ? 1.0f : a);  // std::clamp
             int bin = trunc_i32(fmul(fadd(a, 1.0f), HALF));
             bin = bin < 0 ? 0 : (NB - 1 < bin ? NB - 1 : bin);
+            if (PACK) {
+                const uint64_t inc = (uint64_t)c.vote << (16 * (bin & 3));
 #pragma unroll
-            for (int k = 0; k < NB; ++k) bins[k] += (bin == k) ? (uint32_t)c.vote : 0u;
+                for (int w = 0; w < NW; ++w) pk[w] += ((bin >> 2) == w) ? inc : 0ull;
+            } else {
+#pragma unroll
+                for (int k = 0; k < NB; ++k) bins[k] += (bin == k) ? (uint32_t)c.vote : 0u;
+            }
         }
     }
     if (!valid) return;
+    if (PACK) {
+#pragma unroll
+        for (int k = 0; k < NB; ++k) bins[k] = (uint32_t)(pk[k >> 2] >> (16 * (k & 3))) & 0xffffu;
+    }
     uint32_t* row = out + i * NB;
     if (NB == 8) {
         reinterpret_cast<uint4*>(row)[0] = make_uint4(bins[0], bins[1], bins[2], bins[3]);
@@ -222,6 +259,25 @@ int build_pyramids_dev(tgvg_ctx* ctx, const tgvg_camera* cams, int32_t ncam, flo
     return TGVG_OK;
 }
 
+// The binning launch: the packed counters when no cube can collect more than
+// 65535 votes (every camera's vote counted once), else the per-bin counters.
+static void launch_histograms(const tgvg_camera* cams, int32_t ncam, unsigned grid, cudaStream_t s,
+                              const uint4* cubes, int64_t n, const DevCam* d_cams, const float* tex, const float* o,
+                              float r_root, Thresholds thr, int32_t nbins, uint32_t* out) {
+    finish_thresholds(thr);
+    int64_t votes = 0;
+    for (int c = 0; c < ncam; ++c) votes += cams[c].lidar ? 5 : 1;
+    const bool pack = votes <= 65535;
+#define TGVG_HIST(NBV, PK) \
+    k_histograms<NBV, PK><<<grid, HIST_BLOCK, 0, s>>>(cubes, n, d_cams, ncam, tex, o[0], o[1], o[2], r_root, thr, out)
+    if (nbins == 8) {
+        if (pack) TGVG_HIST(8, true); else TGVG_HIST(8, false);
+    } else {
+        if (pack) TGVG_HIST(10, true); else TGVG_HIST(10, false);
+    }
+#undef TGVG_HIST
+}
+
 int histograms_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, int64_t n, const tgvg_camera* cams,
                    int32_t ncam, const float* d_levels, const int64_t* level_offset,
                    const float origin[3], float r_root, int32_t nbins, uint32_t* d_out) {
@@ -236,14 +292,8 @@ int histograms_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, int64_t n, const tgv
     Thresholds thr;
     std::memcpy(thr.t, ctx->lvl_thresh, sizeof(thr.t));
     const unsigned grid = (unsigned)((n + HIST_BLOCK - 1) / HIST_BLOCK);
-    if (nbins == 8)
-        k_histograms<8><<<grid, HIST_BLOCK, 0, ctx->stream>>>(
-            reinterpret_cast<const uint4*>(d_cubes), n, d_cams, ncam, d_levels, origin[0], origin[1],
-            origin[2], r_root, thr, d_out);
-    else
-        k_histograms<10><<<grid, HIST_BLOCK, 0, ctx->stream>>>(
-            reinterpret_cast<const uint4*>(d_cubes), n, d_cams, ncam, d_levels, origin[0], origin[1],
-            origin[2], r_root, thr, d_out);
+    launch_histograms(cams, ncam, grid, ctx->stream, reinterpret_cast<const uint4*>(d_cubes), n, d_cams, d_levels,
+                      origin, r_root, thr, nbins, d_out);
     TGVG_LAUNCHED(ctx);
     return TGVG_OK;
 }
@@ -453,11 +503,7 @@ extern "C" int tgvg_compute_histograms_noalloc(const tgvg_cube* d_cubes, int64_t
     Thresholds thr;
     tgvg_level_thresholds(thr.t);
     const unsigned grid = (unsigned)((n + HIST_BLOCK - 1) / HIST_BLOCK);
-    if (nbins == 8)
-        k_histograms<8><<<grid, HIST_BLOCK, 0, s>>>(reinterpret_cast<const uint4*>(d_cubes), n, d_cams, ncam, d_tex,
-                                                    origin[0], origin[1], origin[2], r_root, thr, d_out);
-    else
-        k_histograms<10><<<grid, HIST_BLOCK, 0, s>>>(reinterpret_cast<const uint4*>(d_cubes), n, d_cams, ncam,
-                                                     d_tex, origin[0], origin[1], origin[2], r_root, thr, d_out);
+    launch_histograms(cams, ncam, grid, s, reinterpret_cast<const uint4*>(d_cubes), n, d_cams, d_tex, origin, r_root,
+                      thr, nbins, d_out);
     return cudaGetLastError() == cudaSuccess ? TGVG_OK : TGVG_ERR_CUDA;
 }
