@@ -791,6 +791,35 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_cluster(IterArgs a) {
     }
 }
 
+// Every iteration of one tiny level in ONE launch of ONE block of 1024 threads:
+// as k_level_cluster with __syncthreads in place of the cluster barrier.  All
+// readers and writers share one SM, so the sweeps read through L1 (plain loads:
+// a block's global writes are visible to the block after __syncthreads), and
+// a level of up to a couple of thousand cubes stays in L1 for all its
+// iterations.
+template <int MODE, bool STOP>
+__global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_cta(IterArgs a) {
+    const int beg = a.o, end = a.o + a.n;
+    for (int i = 0; i < a.iters; ++i) {
+        const int it = a.it0 + i;
+        if (STOP && MODE != M_STREAM && *(volatile int*)(a.done + a.slot0)) break;
+        const bool res = STOP && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
+        WarpAcc wd, wp;
+        if (res) sweep<MODE, true, STOP, false, true, false>(a, beg, end, wd);
+        else sweep<MODE, false, STOP, false, true, false>(a, beg, end, wd);
+        if (res) wd.flush(a.acc, 1, threadIdx.x & 31);
+        __syncthreads();
+        if (res) sweep<MODE, true, STOP, false, false, false>(a, beg, end, wp);
+        else sweep<MODE, false, STOP, false, false, false>(a, beg, end, wp);
+        if (res) {
+            wp.flush(a.acc, 0, threadIdx.x & 31);
+            __syncthreads();
+            check_slots<MODE>(a, it);
+        }
+        __syncthreads();
+    }
+}
+
 // Stopping test after a residual iteration: relative fixed-point residual
 // (|x+ - x| + |y+ - y|) / (|x+| + |y+|) in FP64 per slot (sigma = tau).
 __global__ void k_check(int s0, int ns, double* __restrict__ acc, int* __restrict__ done, float tol, int iter,
@@ -1517,6 +1546,8 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 //   in-memory and streaming semantics (OC semantics run cfg 14 instead).
 // cfg 19: as 18 with the tiles' contiguous streams staged by TMA bulk copies
 //   (k_fused_tma).
+// cfg 22: every iteration in one launch of a single 1024-thread block
+//   (k_level_cta), reading through L1, for units of up to 4096 cubes.
 // cfg 20 / 21: one ordered-wavefront launch per iteration (k_wave): each
 //   block runs the dual then the primal step of a group of 512-cube tiles,
 //   after the tiles the primal step depends on have published their dual
@@ -1532,7 +1563,8 @@ static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
 static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13, CFG_BAND = 14, CFG_BAND_SWAP = 15;
 static constexpr int CFG_BAND_ILP = 16, CFG_BAND_SWAP_ILP = 17, CFG_FUSED = 18, CFG_FUSED_TMA = 19;
-static constexpr int CFG_WAVE = 20, CFG_WAVE_L1 = 21;
+static constexpr int CFG_WAVE = 20, CFG_WAVE_L1 = 21, CFG_CTA = 22;
+static constexpr int CTA_MAX_N = 4096;  // the single-block schedule is a candidate up to this unit size
 static inline bool fused_cfg(int cfg) { return cfg == CFG_FUSED || cfg == CFG_FUSED_TMA; }
 static inline bool wave_cfg(int cfg) { return cfg == CFG_WAVE || cfg == CFG_WAVE_L1; }
 
@@ -1798,6 +1830,16 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
         }
         return TGVG_OK;
     }
+    if (cfg == CFG_CTA) {
+        a.chunk = a.n;
+        a.it0 = it0;
+        a.iters = count;
+        a.pf = a.swap = a.band = 0;
+        if (stop) k_level_cta<MODE, true><<<1, CLUSTER_BLOCK, 0, ctx->stream>>>(a);
+        else k_level_cta<MODE, false><<<1, CLUSTER_BLOCK, 0, ctx->stream>>>(a);
+        TGVG_LAUNCHED(ctx);
+        return TGVG_OK;
+    }
     if (cfg == CFG_CLUSTER8 || cfg == CFG_CLUSTER16) {
         const int cs = cfg == CFG_CLUSTER16 ? 16 : 8;
         int cmax = 0;
@@ -1855,6 +1897,7 @@ static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& ca
             if (g != last_grid) cands.push_back(k);
             last_grid = g;
         }
+    if (n <= CTA_MAX_N) cands.push_back(CFG_CTA);
     if (n <= CLUSTER_MAX_N) {
         int cs = 0;
         if ((rc = cluster_capacity<MODE>(ctx, stop, &cs))) return rc;
