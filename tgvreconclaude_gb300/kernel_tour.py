@@ -8,8 +8,9 @@ Stages, in order: cubes from the first depth maps (Stage 1), their merge
 (Stage 2) and its 2:1 balance (Stage 3); pyramids and histograms (Stage 5)
 from the workload's depth maps (the first K with --maps); the TGV solve (Stage 6) under the in-memory, OC and streaming semantics
 with each schedule family forced in turn (per-sweep launches, band order, two
-cubes per thread, persistent, cluster, single block, fused, fused with TMA
-staging, ordered wavefront through L2 and through L1); surface
+cubes per thread, persistent, cluster and single block on the small levels
+they are for, fused, fused with TMA staging, ordered
+wavefront through L2 and through L1); surface
 extraction with normals; the warm-start network's features, forward pass,
 gradient and one training epoch.  Prints one line per stage.
 """
@@ -54,7 +55,10 @@ def main(argv=None):
     state = None
     for mode in ("inmem", "oc", "stream"):
         for cfg_id in (0, 14, 16, 3, 11, 22, 18, 19, 20, 21):
-            ctx.set_schedule(mode, -1, cfg_id)
+            ctx.set_schedule(mode, -1, 14 if cfg_id in (11, 22) else cfg_id)
+            if cfg_id in (11, 22):  # the small-level schedules on the levels they are for
+                for cls in range(13 if cfg_id == 22 else 17):
+                    ctx.set_schedule(mode, cls, cfg_id)
             out, st = api.tgv_solve(w.cubes, hists, None if mode == "inmem" else leaves, mode, prm)
             if mode == "inmem" and cfg_id == 0:
                 state = out
