@@ -172,8 +172,10 @@ int tgvg_set_timing(tgvg_ctx* ctx, int on);
  * point to earlier tiles once short runs of tiles are grouped, which holds for
  * Morton-sorted cubes; otherwise 14; never chosen by the autotuner), 22 = one
  * launch of a single 1024-thread block running every iteration, reading through
- * L1 (units of at most 4096 cubes), -1 = let the online autotuner choose
- * (default).  Results do not depend on it. */
+ * L1 (units of at most 4096 cubes), 23 = as 22 with the unit's state held in
+ * shared memory for the whole launch (units of at most 2048 cubes; larger
+ * units run 22), -1 = let the online autotuner choose (default).  Results do
+ * not depend on it. */
 int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
 /* CUDA graphs for the level loop (1 = on, the default; 0 = off).  When every
  * level's schedule is already fixed (chosen by the autotuner in an earlier

@@ -522,7 +522,7 @@ __device__ __forceinline__ void primal_load(const IterArgs& a, int p, PrimalLd& 
 }
 
 template <bool RES>
-__device__ __forceinline__ void primal_finish(const IterArgs& a, int p, const PrimalLd& L, double& dd, double& nd) {
+__device__ __forceinline__ void primal_math(const PrimalLd& L, float4& uvn, float4& barn, double& dd, double& nd) {
     const float4 U = L.U, P = L.P, Q = L.Q;
     const float q5 = L.q5;
     const float2 D = L.D;
@@ -545,14 +545,22 @@ __device__ __forceinline__ void primal_finish(const IterArgs& a, int p, const Pr
     const float vxn = fadd(U.y, fmul(0.25f, fadd(p0, dqx)));
     const float vyn = fadd(U.z, fmul(0.25f, fadd(p1, dqy)));
     const float vzn = fadd(U.w, fmul(0.25f, fadd(p2, dqz)));
-    a.bar[p] = make_float4(fsub(fmul(2.0f, un), U.x), fsub(fmul(2.0f, vxn), U.y), fsub(fmul(2.0f, vyn), U.z),
-                           fsub(fmul(2.0f, vzn), U.w));
-    a.uv[p] = make_float4(un, vxn, vyn, vzn);
+    barn = make_float4(fsub(fmul(2.0f, un), U.x), fsub(fmul(2.0f, vxn), U.y), fsub(fmul(2.0f, vyn), U.z),
+                       fsub(fmul(2.0f, vzn), U.w));
+    uvn = make_float4(un, vxn, vyn, vzn);
     if (RES) {
         const double d0 = (double)un - U.x, d1 = (double)vxn - U.y, d2 = (double)vyn - U.z, d3 = (double)vzn - U.w;
         dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
         nd = (double)un * un + (double)vxn * vxn + (double)vyn * vyn + (double)vzn * vzn;
     }
+}
+
+template <bool RES>
+__device__ __forceinline__ void primal_finish(const IterArgs& a, int p, const PrimalLd& L, double& dd, double& nd) {
+    float4 uvn, barn;
+    primal_math<RES>(L, uvn, barn, dd, nd);
+    a.bar[p] = barn;
+    a.uv[p] = uvn;
 }
 
 template <int MODE, bool RES, bool CG>
@@ -974,6 +982,128 @@ __device__ __forceinline__ void dual_res(const DualLd& L, const float4& Po, cons
     dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5 + d6 * d6 + d7 * d7 + d8 * d8;
     nd = (double)Po.x * Po.x + (double)Po.y * Po.y + (double)Po.z * Po.z + (double)Po.w * Po.w +
          (double)Qo.x * Qo.x + (double)Qo.y * Qo.y + (double)Qo.z * Qo.z + (double)Qo.w * Qo.w + (double)q5n * q5n;
+}
+
+// ---- tiny levels in shared memory (schedule 23) -------------------------------
+// Every iteration of a unit of at most SMEM_MAX_N cubes in ONE launch of ONE
+// 1024-thread block that holds the unit's state, data term and neighbour
+// indices in shared memory (100 B per cube) for the whole launch: loaded once,
+// iterated with __syncthreads between the sweeps, written back once.  Cubes
+// outside the unit (coarser levels, the snapshot, other leaves) are read from
+// global memory; nothing writes them during the launch.  The arithmetic is the
+// split kernels' (dual_math, primal_math).
+constexpr int SMEM_MAX_N = 2048;
+static inline size_t smem_level_bytes(int n) { return size_t(n) * 100; }
+
+template <int MODE>
+__device__ __forceinline__ float4 smem_bar(const IterArgs& a, const float4* s_bar, int j, const float4& own) {
+    if (j < 0) return own;
+    if (MODE != M_INMEM && (j & BORDER)) return a.snap[j & POS_MASK];
+    const unsigned li = (unsigned)(j - a.o);
+    return li < (unsigned)a.n ? s_bar[li] : a.bar[j];
+}
+
+template <int MODE>
+__device__ __forceinline__ bool smem_pq(const IterArgs& a, const float4* s_P, const float4* s_Q, const float* s_q5,
+                                        int jf, float4& A, float4& B, float& c5) {
+    if (jf < 0 || (MODE == M_STREAM && (jf & BORDER))) return false;
+    const int j = jf & POS_MASK;
+    const unsigned li = (unsigned)(j - a.o);
+    if (li < (unsigned)a.n) { A = s_P[li]; B = s_Q[li]; c5 = s_q5[li]; }
+    else { A = a.P4[j]; B = a.Q4[j]; c5 = a.Q1[j]; }
+    return true;
+}
+
+template <int MODE, bool STOP>
+__global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_smem(IterArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = a.n, o = a.o;
+    float4* s_uv = reinterpret_cast<float4*>(smem_raw);
+    float4* s_bar = s_uv + n;
+    float4* s_P = s_bar + n;
+    float4* s_Q = s_P + n;
+    float2* s_dat = reinterpret_cast<float2*>(s_Q + n);
+    float* s_q5 = reinterpret_cast<float*>(s_dat + n);
+    int* s_nb = reinterpret_cast<int*>(s_q5 + n);  // [6][n]
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int p = o + i;
+        s_uv[i] = a.uv[p]; s_bar[i] = a.bar[p]; s_P[i] = a.P4[p]; s_Q[i] = a.Q4[p];
+        s_dat[i] = a.dat[p]; s_q5[i] = a.Q1[p];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) s_nb[f * n + i] = a.nb[(size_t)f * a.npos + p];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (int k = 0; k < a.iters; ++k) {
+        const int it = a.it0 + k;
+        if (STOP && MODE != M_STREAM && *(volatile int*)(a.done + a.slot0)) break;
+        const bool res = STOP && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
+        WarpAcc wd, wp;
+        for (int i0 = 0; i0 < n; i0 += blockDim.x) {  // dual sweep (tgv.cpp:158-189)
+            const int i = i0 + (int)threadIdx.x;
+            bool work = i < n;
+            int slot = -1;
+            if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + o + i) : a.slot0;
+            if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
+            double dd = 0.0, nd = 0.0;
+            if (work) {
+                DualLd L;
+                L.b = s_bar[i]; L.P = s_P[i]; L.Q = s_Q[i]; L.q5 = s_q5[i];
+                L.B0 = smem_bar<MODE>(a, s_bar, s_nb[i], L.b);
+                L.B2 = smem_bar<MODE>(a, s_bar, s_nb[2 * n + i], L.b);
+                L.B4 = smem_bar<MODE>(a, s_bar, s_nb[4 * n + i], L.b);
+                float4 Po, Qo;
+                float q5n;
+                dual_math(a, L, Po, Qo, q5n);
+                if (res) dual_res(L, Po, Qo, q5n, dd, nd);
+                s_P[i] = Po; s_Q[i] = Qo; s_q5[i] = q5n;
+            }
+            if (res) wd.add(work ? slot : -1, dd, nd, a.acc, 1, lane);
+        }
+        if (res) wd.flush(a.acc, 1, lane);
+        __syncthreads();
+        for (int i0 = 0; i0 < n; i0 += blockDim.x) {  // primal sweep (tgv.cpp:191-230)
+            const int i = i0 + (int)threadIdx.x;
+            bool work = i < n;
+            int slot = -1;
+            if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + o + i) : a.slot0;
+            if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
+            double dd = 0.0, nd = 0.0;
+            if (work) {
+                PrimalLd L;
+                L.U = s_uv[i]; L.P = s_P[i]; L.Q = s_Q[i]; L.q5 = s_q5[i]; L.D = s_dat[i];
+                L.gp10 = L.gq10 = L.gq13 = L.gq14 = 0.f;
+                L.gp31 = L.gq31 = L.gq33 = L.gq35 = 0.f;
+                L.gp52 = L.gq52 = L.gq54 = L.gq55 = 0.f;
+                float4 A, B;
+                float c5;
+                if (smem_pq<MODE>(a, s_P, s_Q, s_q5, s_nb[n + i], A, B, c5)) {
+                    L.gp10 = A.x; L.gq10 = A.w; L.gq13 = B.z; L.gq14 = B.w;
+                }
+                if (smem_pq<MODE>(a, s_P, s_Q, s_q5, s_nb[3 * n + i], A, B, c5)) {
+                    L.gp31 = A.y; L.gq31 = B.x; L.gq33 = B.z; L.gq35 = c5;
+                }
+                if (smem_pq<MODE>(a, s_P, s_Q, s_q5, s_nb[5 * n + i], A, B, c5)) {
+                    L.gp52 = A.z; L.gq52 = B.y; L.gq54 = B.w; L.gq55 = c5;
+                }
+                float4 uvn, barn;
+                if (res) primal_math<true>(L, uvn, barn, dd, nd);
+                else primal_math<false>(L, uvn, barn, dd, nd);
+                s_uv[i] = uvn; s_bar[i] = barn;
+            }
+            if (res) wp.add(work ? slot : -1, dd, nd, a.acc, 0, lane);
+        }
+        if (res) {
+            wp.flush(a.acc, 0, lane);
+            __syncthreads();
+            check_slots<MODE>(a, it);
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int p = o + i;
+        a.uv[p] = s_uv[i]; a.bar[p] = s_bar[i]; a.P4[p] = s_P[i]; a.Q4[p] = s_Q[i]; a.Q1[p] = s_q5[i];
+    }
 }
 
 // The primal's neighbour p/q of faces 1/3/5 from their slots: shared memory
@@ -1548,6 +1678,8 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 //   (k_fused_tma).
 // cfg 22: every iteration in one launch of a single 1024-thread block
 //   (k_level_cta), reading through L1, for units of up to 4096 cubes.
+// cfg 23: as 22 with the unit's state, data term and neighbour indices held in
+//   shared memory for the whole launch (k_level_smem), units of up to 2048 cubes.
 // cfg 20 / 21: one ordered-wavefront launch per iteration (k_wave): each
 //   block runs the dual then the primal step of a group of 512-cube tiles,
 //   after the tiles the primal step depends on have published their dual
@@ -1563,7 +1695,7 @@ static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
 static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13, CFG_BAND = 14, CFG_BAND_SWAP = 15;
 static constexpr int CFG_BAND_ILP = 16, CFG_BAND_SWAP_ILP = 17, CFG_FUSED = 18, CFG_FUSED_TMA = 19;
-static constexpr int CFG_WAVE = 20, CFG_WAVE_L1 = 21, CFG_CTA = 22;
+static constexpr int CFG_WAVE = 20, CFG_WAVE_L1 = 21, CFG_CTA = 22, CFG_SMEM = 23;
 static constexpr int CTA_MAX_N = 4096;  // the single-block schedule is a candidate up to this unit size
 static inline bool fused_cfg(int cfg) { return cfg == CFG_FUSED || cfg == CFG_FUSED_TMA; }
 static inline bool wave_cfg(int cfg) { return cfg == CFG_WAVE || cfg == CFG_WAVE_L1; }
@@ -1689,6 +1821,21 @@ static int effective_cfg(const tgvg_ctx* ctx, int cfg) {
     if (fused_cfg(cfg) && (MODE == M_OC || !ctx->fuse_cur)) return CFG_BAND;
     if (wave_cfg(cfg) && (MODE == M_OC || !wz || !wz->ok)) return CFG_BAND;
     return cfg;
+}
+
+// Shared-memory limit of the tiny-level kernel, raised once (before any capture).
+template <int MODE>
+static int smem_level_setup(tgvg_ctx* ctx) {
+    if (ctx->smem_level_ready[MODE]) return TGVG_OK;
+    const int bytes = (int)smem_level_bytes(SMEM_MAX_N);
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_level_smem<MODE, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute((const void*)k_level_smem<MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 bytes);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "shared memory limit");
+    ctx->smem_level_ready[MODE] = true;
+    return TGVG_OK;
 }
 
 // Blocks per SM of the wavefront kernel.
@@ -1830,6 +1977,18 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
         }
         return TGVG_OK;
     }
+    if (cfg == CFG_SMEM && a.n > SMEM_MAX_N) cfg = CFG_CTA;
+    if (cfg == CFG_SMEM) {
+        const int rc = smem_level_setup<MODE>(ctx);
+        if (rc) return rc;
+        a.it0 = it0;
+        a.iters = count;
+        const size_t sh = smem_level_bytes(a.n);
+        if (stop) k_level_smem<MODE, true><<<1, CLUSTER_BLOCK, sh, ctx->stream>>>(a);
+        else k_level_smem<MODE, false><<<1, CLUSTER_BLOCK, sh, ctx->stream>>>(a);
+        TGVG_LAUNCHED(ctx);
+        return TGVG_OK;
+    }
     if (cfg == CFG_CTA) {
         a.chunk = a.n;
         a.it0 = it0;
@@ -1898,6 +2057,10 @@ static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& ca
             last_grid = g;
         }
     if (n <= CTA_MAX_N) cands.push_back(CFG_CTA);
+    if (n <= SMEM_MAX_N) {
+        if ((rc = smem_level_setup<MODE>(ctx))) return rc;
+        cands.push_back(CFG_SMEM);
+    }
     if (n <= CLUSTER_MAX_N) {
         int cs = 0;
         if ((rc = cluster_capacity<MODE>(ctx, stop, &cs))) return rc;
@@ -1943,6 +2106,7 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
             int cs = 0;
             return cluster_capacity<MODE>(ctx, stop, &cs);
         }
+        if (tuned == CFG_SMEM) return smem_level_setup<MODE>(ctx);
         if (fused_cfg(tuned)) {
             if (MODE == M_OC) *cfg = CFG_BAND;
             int occ = 0;
