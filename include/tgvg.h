@@ -174,8 +174,11 @@ int tgvg_set_timing(tgvg_ctx* ctx, int on);
  * launch of a single 1024-thread block running every iteration, reading through
  * L1 (units of at most 4096 cubes), 23 = as 22 with the unit's state held in
  * shared memory for the whole launch (units of at most 2048 cubes; larger
- * units run 22), -1 = let the online autotuner choose (default).  Results do
- * not depend on it. */
+ * units run 22), 24 = one thread-block cluster of 16 (else 8) CTAs whose
+ * shared memories hold the unit's state, neighbours in other CTAs read through
+ * distributed shared memory (units of at most 16 x 2816 cubes; larger units
+ * run 14), -1 = let the online autotuner choose (default).  Results do not
+ * depend on it. */
 int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
 /* CUDA graphs for the level loop (1 = on, the default; 0 = off).  When every
  * level's schedule is already fixed (chosen by the autotuner in an earlier

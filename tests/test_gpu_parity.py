@@ -187,13 +187,13 @@ def test_tgv_autotuned_schedules_are_exact(oracle_lib):
 
 @pytest.mark.parametrize("mode", ["inmem", "oc", "stream"])
 def test_tgv_every_schedule_is_exact(oracle_lib, mode):
-    """Each of the twenty-four iteration schedules (per-sweep launches with and
+    """Each of the twenty-five iteration schedules (per-sweep launches with and
     without register cap / L2 prefetch / swapped sweep directions / band order /
     two cubes per thread, the fused tile kernel plain and TMA-staged, the ordered
     wavefront through L2 and through L1 (these four run band order in OC
     semantics), six persistent grid sizes, clusters of 8 and 16 CTAs, a single
-    block reading through L1 or holding the state in shared memory), forced for
-    every level,
+    block reading through L1 or holding the state in shared memory, a cluster
+    holding it in distributed shared memory), forced for every level,
     with and without the stopping test, gives the oracle's state bit for bit."""
     ctx = api.context()
     rng = np.random.default_rng(41)
@@ -204,7 +204,7 @@ def test_tgv_every_schedule_is_exact(oracle_lib, mode):
     stop, rst = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 300, tol=1e-3, check_every=10,
                                      nthreads=8)
     try:
-        for cfg in range(24):
+        for cfg in range(25):
             ctx.set_schedule(mode, -1, cfg)
             out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=40))
             want = 14 if (18 <= cfg <= 21 and mode == "oc") else cfg

@@ -78,7 +78,7 @@ extern "C" void tgvg_level_thresholds(float* t13) {
 }
 
 extern "C" int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg) {
-    if (!ctx || mode < 0 || mode > 2 || cls < -1 || cls > 31 || cfg < -1 || cfg > 23) return TGVG_ERR_INVALID;
+    if (!ctx || mode < 0 || mode > 2 || cls < -1 || cls > 31 || cfg < -1 || cfg > 24) return TGVG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     for (int c = 0; c < 32; ++c)
         if (cls < 0 || c == cls) ctx->tune[mode][c] = cfg;

@@ -1106,6 +1106,152 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_smem(IterArgs a) {
     }
 }
 
+// ---- small levels in distributed shared memory (schedule 24) -------------------
+// As k_level_smem for a unit of up to DSM_MAX_CHUNK cubes per CTA of one
+// thread-block cluster (8 or 16 CTAs of 1024 threads): each CTA holds the
+// state and data term of its contiguous chunk in its own shared memory (76 B
+// per cube; the neighbour indices stay in global memory), and a neighbour in
+// another CTA's chunk is read from that CTA's shared memory through the
+// cluster's distributed shared memory.  The hardware cluster barrier orders
+// the sweeps and makes each CTA's shared-memory writes visible to the others;
+// the last barrier of every iteration also keeps every CTA's shared memory
+// alive until no other CTA reads it.
+constexpr int DSM_MAX_CHUNK = 2816;
+static inline size_t dsm_level_bytes(int chunk) { return size_t(chunk) * 76; }
+
+struct DsmView {  // this CTA's arrays; a remote rank's through map_shared_rank
+    float4* uv; float4* bar; float4* P; float4* Q; float2* dat; float* q5;
+};
+
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// Generic address of the same shared-memory location in CTA `rank` of the cluster.
+template <class T>
+__device__ __forceinline__ T* dsm_map(T* p, unsigned rank) {
+    unsigned long long in = (unsigned long long)p, out;
+    asm volatile("mapa.u64 %0, %1, %2;" : "=l"(out) : "l"(in), "r"(rank));
+    return reinterpret_cast<T*>(out);
+}
+
+template <int MODE>
+__device__ __forceinline__ float4 dsm_bar(const IterArgs& a, const DsmView& v, int chunk, unsigned me, int j,
+                                          const float4& own) {
+    if (j < 0) return own;
+    if (MODE != M_INMEM && (j & BORDER)) return a.snap[j & POS_MASK];
+    const unsigned li = (unsigned)(j - a.o);
+    if (li >= (unsigned)a.n) return a.bar[j];
+    const unsigned r = li / (unsigned)chunk, l = li - r * (unsigned)chunk;
+    return r == me ? v.bar[l] : dsm_map(v.bar, r)[l];
+}
+
+template <int MODE>
+__device__ __forceinline__ bool dsm_pq(const IterArgs& a, const DsmView& v, int chunk, unsigned me, int jf, float4& A,
+                                       float4& B, float& c5) {
+    if (jf < 0 || (MODE == M_STREAM && (jf & BORDER))) return false;
+    const int j = jf & POS_MASK;
+    const unsigned li = (unsigned)(j - a.o);
+    if (li >= (unsigned)a.n) { A = a.P4[j]; B = a.Q4[j]; c5 = a.Q1[j]; return true; }
+    const unsigned r = li / (unsigned)chunk, l = li - r * (unsigned)chunk;
+    if (r == me) { A = v.P[l]; B = v.Q[l]; c5 = v.q5[l]; }
+    else { A = dsm_map(v.P, r)[l]; B = dsm_map(v.Q, r)[l]; c5 = dsm_map(v.q5, r)[l]; }
+    return true;
+}
+
+template <int MODE, bool STOP>
+__global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_dsm(IterArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int chunk = a.chunk;
+    const unsigned me = cluster_rank();
+    DsmView v;
+    v.uv = reinterpret_cast<float4*>(smem_raw);
+    v.bar = v.uv + chunk;
+    v.P = v.bar + chunk;
+    v.Q = v.P + chunk;
+    v.dat = reinterpret_cast<float2*>(v.Q + chunk);
+    v.q5 = reinterpret_cast<float*>(v.dat + chunk);
+    const int beg = a.o + (int)me * chunk, cnt = max(0, min(chunk, a.o + a.n - beg));
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const int p = beg + i;
+        v.uv[i] = a.uv[p]; v.bar[i] = a.bar[p]; v.P[i] = a.P4[p]; v.Q[i] = a.Q4[p];
+        v.dat[i] = a.dat[p]; v.q5[i] = a.Q1[p];
+    }
+    cluster_barrier();
+    const int lane = threadIdx.x & 31;
+    for (int k = 0; k < a.iters; ++k) {
+        const int it = a.it0 + k;
+        if (STOP && MODE != M_STREAM && *(volatile int*)(a.done + a.slot0)) break;
+        const bool res = STOP && ((it + 1) % a.check_every == 0 || it + 1 == a.iters_total);
+        WarpAcc wd, wp;
+        for (int i0 = 0; i0 < cnt; i0 += blockDim.x) {  // dual sweep (tgv.cpp:158-189)
+            const int i = i0 + (int)threadIdx.x, p = beg + i;
+            bool work = i < cnt;
+            int slot = -1;
+            if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
+            if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
+            double dd = 0.0, nd = 0.0;
+            if (work) {
+                DualLd L;
+                L.b = v.bar[i]; L.P = v.P[i]; L.Q = v.Q[i]; L.q5 = v.q5[i];
+                L.B0 = dsm_bar<MODE>(a, v, chunk, me, __ldg(a.nb + p), L.b);
+                L.B2 = dsm_bar<MODE>(a, v, chunk, me, __ldg(a.nb + 2 * a.npos + p), L.b);
+                L.B4 = dsm_bar<MODE>(a, v, chunk, me, __ldg(a.nb + 4 * a.npos + p), L.b);
+                float4 Po, Qo;
+                float q5n;
+                dual_math(a, L, Po, Qo, q5n);
+                if (res) dual_res(L, Po, Qo, q5n, dd, nd);
+                v.P[i] = Po; v.Q[i] = Qo; v.q5[i] = q5n;
+            }
+            if (res) wd.add(work ? slot : -1, dd, nd, a.acc, 1, lane);
+        }
+        if (res) wd.flush(a.acc, 1, lane);
+        cluster_barrier();
+        for (int i0 = 0; i0 < cnt; i0 += blockDim.x) {  // primal sweep (tgv.cpp:191-230)
+            const int i = i0 + (int)threadIdx.x, p = beg + i;
+            bool work = i < cnt;
+            int slot = -1;
+            if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
+            if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
+            double dd = 0.0, nd = 0.0;
+            if (work) {
+                PrimalLd L;
+                L.U = v.uv[i]; L.P = v.P[i]; L.Q = v.Q[i]; L.q5 = v.q5[i]; L.D = v.dat[i];
+                L.gp10 = L.gq10 = L.gq13 = L.gq14 = 0.f;
+                L.gp31 = L.gq31 = L.gq33 = L.gq35 = 0.f;
+                L.gp52 = L.gq52 = L.gq54 = L.gq55 = 0.f;
+                float4 A, B;
+                float c5;
+                if (dsm_pq<MODE>(a, v, chunk, me, __ldg(a.nb + a.npos + p), A, B, c5)) {
+                    L.gp10 = A.x; L.gq10 = A.w; L.gq13 = B.z; L.gq14 = B.w;
+                }
+                if (dsm_pq<MODE>(a, v, chunk, me, __ldg(a.nb + 3 * a.npos + p), A, B, c5)) {
+                    L.gp31 = A.y; L.gq31 = B.x; L.gq33 = B.z; L.gq35 = c5;
+                }
+                if (dsm_pq<MODE>(a, v, chunk, me, __ldg(a.nb + 5 * a.npos + p), A, B, c5)) {
+                    L.gp52 = A.z; L.gq52 = B.y; L.gq54 = B.w; L.gq55 = c5;
+                }
+                float4 uvn, barn;
+                if (res) primal_math<true>(L, uvn, barn, dd, nd);
+                else primal_math<false>(L, uvn, barn, dd, nd);
+                v.uv[i] = uvn; v.bar[i] = barn;
+            }
+            if (res) wp.add(work ? slot : -1, dd, nd, a.acc, 0, lane);
+        }
+        if (res) {
+            wp.flush(a.acc, 0, lane);
+            cluster_barrier();
+            if (me == 0) check_slots<MODE>(a, it);
+        }
+        cluster_barrier();
+    }
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const int p = beg + i;
+        a.uv[p] = v.uv[i]; a.bar[p] = v.bar[i]; a.P4[p] = v.P[i]; a.Q4[p] = v.Q[i]; a.Q1[p] = v.q5[i];
+    }
+}
+
 // The primal's neighbour p/q of faces 1/3/5 from their slots: shared memory
 // (tile or halo), zero (none / border), or set 0 of global memory (another level).
 __device__ __forceinline__ void fused_gather(const IterArgs& a, const float4* sP, const float4* sQ, const float* s5,
@@ -1680,6 +1826,9 @@ static int iter_occupancy(tgvg_ctx* ctx) {
 //   (k_level_cta), reading through L1, for units of up to 4096 cubes.
 // cfg 23: as 22 with the unit's state, data term and neighbour indices held in
 //   shared memory for the whole launch (k_level_smem), units of up to 2048 cubes.
+// cfg 24: one thread-block cluster of 16 (else 8) CTAs whose shared memories
+//   hold the unit's state, neighbours in other CTAs read through distributed
+//   shared memory (k_level_dsm), units of up to 16 (8) x 2816 cubes.
 // cfg 20 / 21: one ordered-wavefront launch per iteration (k_wave): each
 //   block runs the dual then the primal step of a group of 512-cube tiles,
 //   after the tiles the primal step depends on have published their dual
@@ -1695,7 +1844,7 @@ static constexpr int CFG_LEAN = 7;
 static constexpr int CFG_PF = 8, CFG_LEAN_PF = 9;
 static constexpr int CFG_SWAP = 12, CFG_SWAP_PF = 13, CFG_BAND = 14, CFG_BAND_SWAP = 15;
 static constexpr int CFG_BAND_ILP = 16, CFG_BAND_SWAP_ILP = 17, CFG_FUSED = 18, CFG_FUSED_TMA = 19;
-static constexpr int CFG_WAVE = 20, CFG_WAVE_L1 = 21, CFG_CTA = 22, CFG_SMEM = 23;
+static constexpr int CFG_WAVE = 20, CFG_WAVE_L1 = 21, CFG_CTA = 22, CFG_SMEM = 23, CFG_DSM = 24;
 static constexpr int CTA_MAX_N = 4096;  // the single-block schedule is a candidate up to this unit size
 static inline bool fused_cfg(int cfg) { return cfg == CFG_FUSED || cfg == CFG_FUSED_TMA; }
 static inline bool wave_cfg(int cfg) { return cfg == CFG_WAVE || cfg == CFG_WAVE_L1; }
@@ -1816,10 +1965,15 @@ static int fused_occupancy(tgvg_ctx* ctx, bool tma, int* out) {
 // tables (in-memory and streaming semantics; for the wavefront, a level whose
 // dependencies all point backwards), else band order.
 template <int MODE>
-static int effective_cfg(const tgvg_ctx* ctx, int cfg) {
+static int effective_cfg(const tgvg_ctx* ctx, int cfg, int n) {
     const WaveSet* wz = static_cast<const WaveSet*>(ctx->wave_cur);
     if (fused_cfg(cfg) && (MODE == M_OC || !ctx->fuse_cur)) return CFG_BAND;
     if (wave_cfg(cfg) && (MODE == M_OC || !wz || !wz->ok)) return CFG_BAND;
+    if (cfg == CFG_SMEM && n > SMEM_MAX_N) return CFG_CTA;
+    if (cfg == CFG_DSM) {  // the cluster size is known once dsm_capacity ran (plan and tuning call it)
+        const int cs = ctx->dsm_max[MODE];
+        if (cs >= 0 && (cs == 0 || n > cs * DSM_MAX_CHUNK)) return CFG_BAND;
+    }
     return cfg;
 }
 
@@ -1835,6 +1989,52 @@ static int smem_level_setup(tgvg_ctx* ctx) {
                                  bytes);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "shared memory limit");
     ctx->smem_level_ready[MODE] = true;
+    return TGVG_OK;
+}
+
+// Cluster size of the distributed-shared-memory kernel (16 when the device
+// runs such clusters with the full shared-memory carve-out, else 8, else 0),
+// with the kernel's attributes set; cached in the context.
+template <int MODE>
+static int dsm_capacity(tgvg_ctx* ctx, int* out) {
+    int& c = ctx->dsm_max[MODE];
+    if (c < 0) {
+        c = 0;
+        const int bytes = (int)dsm_level_bytes(DSM_MAX_CHUNK);
+        const void* ks[2] = {(const void*)k_level_dsm<MODE, false>, (const void*)k_level_dsm<MODE, true>};
+        bool ok = true;
+        for (const void* k : ks)
+            ok = ok && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+        } else {
+            for (int cs : {16, 8}) {
+                bool allowed = true;
+                if (cs == 16)
+                    for (const void* k : ks)
+                        allowed = allowed &&
+                                  cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+                if (!allowed) { cudaGetLastError(); continue; }
+                bool fits = true;
+                for (const void* k : ks) {
+                    cudaLaunchConfig_t lc = {};
+                    lc.gridDim = dim3(cs);
+                    lc.blockDim = dim3(CLUSTER_BLOCK);
+                    lc.dynamicSmemBytes = (size_t)bytes;
+                    cudaLaunchAttribute at[1];
+                    at[0].id = cudaLaunchAttributeClusterDimension;
+                    at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+                    lc.attrs = at;
+                    lc.numAttrs = 1;
+                    int nc = 0;
+                    fits = fits && cudaOccupancyMaxActiveClusters(&nc, k, &lc) == cudaSuccess && nc > 0;
+                }
+                if (fits) { c = cs; break; }
+                cudaGetLastError();
+            }
+        }
+    }
+    *out = c;
     return TGVG_OK;
 }
 
@@ -1865,7 +2065,7 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
     if (count <= 0) return TGVG_OK;
     const FuseSet* fz = static_cast<const FuseSet*>(ctx->fuse_cur);
     const WaveSet* wz = static_cast<const WaveSet*>(ctx->wave_cur);
-    cfg = effective_cfg<MODE>(ctx, cfg);
+    cfg = effective_cfg<MODE>(ctx, cfg, a.n);
     if (wave_cfg(cfg)) {
         const bool l1 = cfg == CFG_WAVE_L1;
         int occ = 0, rc = wave_occupancy<MODE>(ctx, l1, &occ);
@@ -1977,6 +2177,33 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
         }
         return TGVG_OK;
     }
+    if (cfg == CFG_DSM) {
+        int cs = 0;
+        const int rc = dsm_capacity<MODE>(ctx, &cs);
+        if (rc) return rc;
+        if (cs == 0 || a.n > cs * DSM_MAX_CHUNK) {
+            cfg = CFG_BAND;  // does not fit: band order
+        } else {
+            a.chunk = (a.n + cs - 1) / cs;
+            a.it0 = it0;
+            a.iters = count;
+            cudaLaunchConfig_t lc = {};
+            lc.gridDim = dim3(cs);
+            lc.blockDim = dim3(CLUSTER_BLOCK);
+            lc.dynamicSmemBytes = dsm_level_bytes(a.chunk);
+            lc.stream = ctx->stream;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = cs; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+            lc.attrs = at;
+            lc.numAttrs = 1;
+            cudaError_t e = stop ? cudaLaunchKernelEx(&lc, k_level_dsm<MODE, true>, a)
+                                 : cudaLaunchKernelEx(&lc, k_level_dsm<MODE, false>, a);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "cluster launch");
+            ++ctx->kernels;
+            return TGVG_OK;
+        }
+    }
     if (cfg == CFG_SMEM && a.n > SMEM_MAX_N) cfg = CFG_CTA;
     if (cfg == CFG_SMEM) {
         const int rc = smem_level_setup<MODE>(ctx);
@@ -2061,6 +2288,11 @@ static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& ca
         if ((rc = smem_level_setup<MODE>(ctx))) return rc;
         cands.push_back(CFG_SMEM);
     }
+    if (n <= 16 * DSM_MAX_CHUNK) {
+        int cs = 0;
+        if ((rc = dsm_capacity<MODE>(ctx, &cs))) return rc;
+        if (cs > 0 && n <= cs * DSM_MAX_CHUNK) cands.push_back(CFG_DSM);
+    }
     if (n <= CLUSTER_MAX_N) {
         int cs = 0;
         if ((rc = cluster_capacity<MODE>(ctx, stop, &cs))) return rc;
@@ -2093,7 +2325,7 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
             int occ = 0;
             return fused_occupancy<MODE>(ctx, *cfg == CFG_FUSED_TMA, &occ);
         }
-        *cfg = effective_cfg<MODE>(ctx, *cfg);
+        *cfg = effective_cfg<MODE>(ctx, *cfg, n);
         if (wave_cfg(*cfg)) {
             int occ = 0;
             return wave_occupancy<MODE>(ctx, *cfg == CFG_WAVE_L1, &occ);
@@ -2106,14 +2338,23 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
             int cs = 0;
             return cluster_capacity<MODE>(ctx, stop, &cs);
         }
-        if (tuned == CFG_SMEM) return smem_level_setup<MODE>(ctx);
+        if (tuned == CFG_SMEM) {
+            *cfg = effective_cfg<MODE>(ctx, tuned, n);
+            return smem_level_setup<MODE>(ctx);
+        }
+        if (tuned == CFG_DSM) {
+            int cs = 0;
+            rc = dsm_capacity<MODE>(ctx, &cs);
+            *cfg = effective_cfg<MODE>(ctx, tuned, n);
+            return rc;
+        }
         if (fused_cfg(tuned)) {
             if (MODE == M_OC) *cfg = CFG_BAND;
             int occ = 0;
             return fused_occupancy<MODE>(ctx, tuned == CFG_FUSED_TMA, &occ);
         }
         if (wave_cfg(tuned)) {
-            *cfg = effective_cfg<MODE>(ctx, tuned);
+            *cfg = effective_cfg<MODE>(ctx, tuned, n);
             int occ = 0;
             return wave_cfg(*cfg) ? wave_occupancy<MODE>(ctx, tuned == CFG_WAVE_L1, &occ) : TGVG_OK;
         }
@@ -2148,7 +2389,11 @@ static int run_unit_t(tgvg_ctx* ctx, IterArgs& a, int iters, bool stop, bool tim
         ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, a.n))] = best;
         cfg = best;
     }
-    *used = effective_cfg<MODE>(ctx, cfg);
+    if (cfg == CFG_DSM) {
+        int cs = 0;
+        if ((rc = dsm_capacity<MODE>(ctx, &cs))) return rc;
+    }
+    *used = effective_cfg<MODE>(ctx, cfg, a.n);
     return run_segment<MODE>(ctx, a, cfg, it, iters - it, stop, timed);
 }
 
