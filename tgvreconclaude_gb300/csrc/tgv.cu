@@ -398,6 +398,14 @@ __device__ __forceinline__ void clip6(float* q, float r) {
 // Loads of state that other blocks rewrite while a persistent kernel runs go
 // to L2 (.cg) so no stale L1 line is ever read; the per-launch kernels use
 // ordinary loads.
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while the previous kernel of the stream finishes;
+// pdl_wait() blocks until that kernel has completed and its writes are
+// visible (a no-op for an ordinary launch), and pdl_release() lets the next
+// such kernel start launching its blocks as this one's blocks retire.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <bool CG> __device__ __forceinline__ float4 ld4(const float4* p) { return CG ? __ldcg(p) : *p; }
 template <bool CG> __device__ __forceinline__ float ld1(const float* p) { return CG ? __ldcg(p) : *p; }
 
@@ -669,6 +677,8 @@ __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpA
 // flight); MINB = 6 (the default) allows about 42.
 template <int MODE, bool RES, bool STOP, int MINB, int ILP = 1>
 __global__ void __launch_bounds__(ITER_BLOCK, MINB) k_dual(IterArgs a) {
+    pdl_wait();
+    pdl_release();
     if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
     const int beg = a.o + blockIdx.x * a.chunk;
     const int end = min(a.o + a.n, beg + a.chunk);
@@ -679,6 +689,8 @@ __global__ void __launch_bounds__(ITER_BLOCK, MINB) k_dual(IterArgs a) {
 
 template <int MODE, bool RES, bool STOP, int MINB, int ILP = 1>
 __global__ void __launch_bounds__(ITER_BLOCK, MINB) k_primal(IterArgs a) {
+    pdl_wait();
+    pdl_release();
     if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
     const int blk = gridDim.x - 1 - blockIdx.x;
     const int beg = a.o + blk * a.chunk;
@@ -832,6 +844,8 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_cta(IterArgs a) {
 // (|x+ - x| + |y+ - y|) / (|x+| + |y+|) in FP64 per slot (sigma = tau).
 __global__ void k_check(int s0, int ns, double* __restrict__ acc, int* __restrict__ done, float tol, int iter,
                         int* __restrict__ iters_run, double* __restrict__ resid) {
+    pdl_wait();
+    pdl_release();
     const int s = s0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= s0 + ns || done[s]) return;
     double* q = acc + s * 4;
@@ -1281,6 +1295,8 @@ template <int MODE, bool RES, bool STOP>
 __global__ void __launch_bounds__(FT) k_fused(IterArgs a, FuseArgs f) {
     __shared__ float4 sP[FT + FH], sQ[FT + FH];
     __shared__ float s5[FT + FH];
+    pdl_wait();
+    pdl_release();
     if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
     const int lane = threadIdx.x & 31;
     WarpAcc wd, wp;
@@ -1446,6 +1462,8 @@ template <int MODE, bool RES, bool STOP>
 __global__ void __launch_bounds__(FT) k_fused_tma(IterArgs a, FuseArgs f) {
     extern __shared__ __align__(128) unsigned char dsm[];
     FusedSmem& sm = *reinterpret_cast<FusedSmem*>(dsm);
+    pdl_wait();
+    pdl_release();
     if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
     if (threadIdx.x == 0) {
         mbar_init(&sm.mbar[0]);
@@ -1755,6 +1773,29 @@ __global__ void k_unpermute(int n, const int* __restrict__ inv, const float4* __
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// Launch with programmatic stream serialisation (the kernel calls pdl_wait()
+// before it touches memory): the launch and the first blocks overlap the end
+// of the previous kernel.  Errors surface through cudaGetLastError.
+template <class... KArgs, class... Args>
+static void launch_pdl_smem(void (*k)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                            Args... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(grid);
+    lc.blockDim = dim3(block);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    cudaLaunchKernelEx(&lc, k, args...);
+}
+template <class... KArgs, class... Args>
+static void launch_pdl(void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+    launch_pdl_smem(k, grid, block, 0, s, args...);
+}
+
 template <int MODE>
 static void launch_iter(tgvg_ctx* ctx, IterArgs a, bool res, bool stop, bool dual, bool lean, bool ilp2) {
     // One full wave: as many blocks as fit on the GPU at once (occupancy of the
@@ -1763,18 +1804,20 @@ static void launch_iter(tgvg_ctx* ctx, IterArgs a, bool res, bool stop, bool dua
     const int want = std::max(1, std::min((a.n + ITER_BLOCK - 1) / ITER_BLOCK, occ * ctx->sm_count));
     a.chunk = ((a.n + want - 1) / want + 31) / 32 * 32;
     const unsigned grid = (unsigned)((a.n + a.chunk - 1) / a.chunk);
-#define TGVG_ITER(K)                                                                         \
-    if (ilp2 && res && stop) K<MODE, true, true, 4, 2><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a); \
-    else if (ilp2 && res) K<MODE, true, false, 4, 2><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
-    else if (ilp2 && stop) K<MODE, false, true, 4, 2><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);  \
-    else if (ilp2) K<MODE, false, false, 4, 2><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);         \
-    else if (res && stop) K<MODE, true, true, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
-    else if (res) K<MODE, true, false, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);     \
-    else if (stop) K<MODE, false, true, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);    \
-    else if (lean) K<MODE, false, false, 8><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);   \
-    else K<MODE, false, false, 6><<<grid, ITER_BLOCK, 0, ctx->stream>>>(a);
+    void (*k)(IterArgs);
+#define TGVG_ITER(K)                                      \
+    if (ilp2 && res && stop) k = K<MODE, true, true, 4, 2>; \
+    else if (ilp2 && res) k = K<MODE, true, false, 4, 2>;   \
+    else if (ilp2 && stop) k = K<MODE, false, true, 4, 2>;  \
+    else if (ilp2) k = K<MODE, false, false, 4, 2>;         \
+    else if (res && stop) k = K<MODE, true, true, 6>;       \
+    else if (res) k = K<MODE, true, false, 6>;              \
+    else if (stop) k = K<MODE, false, true, 6>;             \
+    else if (lean) k = K<MODE, false, false, 8>;            \
+    else k = K<MODE, false, false, 6>;
     if (dual) { TGVG_ITER(k_dual) } else { TGVG_ITER(k_primal) }
 #undef TGVG_ITER
+    launch_pdl(k, grid, ITER_BLOCK, ctx->stream, a);
 }
 
 // Blocks per SM of the plain (and register-capped) sweep kernels, per mode.
@@ -2094,8 +2137,8 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
             }
             if (res) {
                 const int ns = unit_slots<MODE>(a.nslot);
-                k_check<<<blocks_for(ns, 128), 128, 0, ctx->stream>>>(a.slot0, ns, a.acc, a.done, a.tol, it,
-                                                                          a.iters_run, a.resid);
+                launch_pdl(k_check, blocks_for(ns, 128), 128, ctx->stream, a.slot0, ns, a.acc, a.done, a.tol, it,
+                           a.iters_run, a.resid);
                 TGVG_LAUNCHED(ctx);
             }
         }
@@ -2119,17 +2162,12 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
             cudaEvent_t* te = mark ? &ctx->tev[3 * (it / TIMING_STRIDE)] : nullptr;
             if (mark) TGVG_CK(ctx, record_event(te[0], ctx->stream, ctx->capturing));
             const size_t sh = tma ? FUSED_TMA_SMEM : 0;
-            if (tma) {
-                if (res && stop) k_fused_tma<MODE, true, true><<<grid, FT, sh, ctx->stream>>>(a, f);
-                else if (res) k_fused_tma<MODE, true, false><<<grid, FT, sh, ctx->stream>>>(a, f);
-                else if (stop) k_fused_tma<MODE, false, true><<<grid, FT, sh, ctx->stream>>>(a, f);
-                else k_fused_tma<MODE, false, false><<<grid, FT, sh, ctx->stream>>>(a, f);
-            } else {
-                if (res && stop) k_fused<MODE, true, true><<<grid, FT, 0, ctx->stream>>>(a, f);
-                else if (res) k_fused<MODE, true, false><<<grid, FT, 0, ctx->stream>>>(a, f);
-                else if (stop) k_fused<MODE, false, true><<<grid, FT, 0, ctx->stream>>>(a, f);
-                else k_fused<MODE, false, false><<<grid, FT, 0, ctx->stream>>>(a, f);
-            }
+            void (*k)(IterArgs, FuseArgs);
+            if (tma) k = res && stop ? k_fused_tma<MODE, true, true> : res ? k_fused_tma<MODE, true, false>
+                         : stop ? k_fused_tma<MODE, false, true> : k_fused_tma<MODE, false, false>;
+            else k = res && stop ? k_fused<MODE, true, true> : res ? k_fused<MODE, true, false>
+                     : stop ? k_fused<MODE, false, true> : k_fused<MODE, false, false>;
+            launch_pdl_smem(k, grid, FT, sh, ctx->stream, a, f);
             TGVG_LAUNCHED(ctx);
             if (mark) {
                 TGVG_CK(ctx, record_event(te[1], ctx->stream, ctx->capturing));
@@ -2137,8 +2175,8 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
             }
             if (res) {
                 const int ns = unit_slots<MODE>(a.nslot);
-                k_check<<<blocks_for(ns, 128), 128, 0, ctx->stream>>>(a.slot0, ns, a.acc, a.done, a.tol, it,
-                                                                          a.iters_run, a.resid);
+                launch_pdl(k_check, blocks_for(ns, 128), 128, ctx->stream, a.slot0, ns, a.acc, a.done, a.tol, it,
+                           a.iters_run, a.resid);
                 TGVG_LAUNCHED(ctx);
             }
         }
@@ -2170,8 +2208,8 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
             ctx->kernels += 2;
             if (res) {
                 const int ns = unit_slots<MODE>(a.nslot);
-                k_check<<<blocks_for(ns, 128), 128, 0, ctx->stream>>>(a.slot0, ns, a.acc, a.done, a.tol, it,
-                                                                          a.iters_run, a.resid);
+                launch_pdl(k_check, blocks_for(ns, 128), 128, ctx->stream, a.slot0, ns, a.acc, a.done, a.tol, it,
+                           a.iters_run, a.resid);
                 TGVG_LAUNCHED(ctx);
             }
         }
