@@ -574,10 +574,11 @@ def run_ours(args):
             "clocks": clk, "graph": last_st["graph"],
             "gpu_launches": int(launches), "leaf_iters_per_step": int(li_all / args.steps),
             "levels_detail": [{"depth": d, "active": int(a), "ms": round(m, 3), "schedule": s, "iters": it,
-                               "residual": r}
-                              for d, a, m, s, it, r in zip(last_st["depth"], last_st["active"], last_st["level_ms"],
-                                                          last_st["schedule"], last_st["iters_run"],
-                                                          last_st["residual"])],
+                               "residual": r, "energy": en}
+                              for d, a, m, s, it, r, en in zip(last_st["depth"], last_st["active"],
+                                                              last_st["level_ms"], last_st["schedule"],
+                                                              last_st["iters_run"], last_st["residual"],
+                                                              last_st["energy"])],
             "gen_s": round(t_gen, 1),
         }
         print(json.dumps(result), flush=True)

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define TGVG_ABI_VERSION 2
+#define TGVG_ABI_VERSION 3
 
 /* ---- status codes -------------------------------------------------------- */
 #define TGVG_OK             0
@@ -128,6 +128,13 @@ typedef struct tgvg_stats {
                                             wavefront kernel (kt_dual_ms holds its time,
                                             kt_primal_ms 0)                                   */
     int32_t reserved;
+    /* No counterpart in the reference: the FP64 primal energy of level slot k's
+     * state when the level ends, sum over its cubes of tot |u - median| +
+     * alpha1 |grad u - v| + alpha0 |e(v)| with the iteration's own difference
+     * operators (a missing neighbour counts as the cube itself; e(v) in Voigt
+     * form, off-diagonals halved and counted once).  Neighbours are read from the
+     * current state in every semantics. */
+    double energy[TGVG_MAX_LEVELS];
 } tgvg_stats;
 
 typedef struct tgvg_ctx tgvg_ctx;

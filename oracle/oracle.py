@@ -209,7 +209,7 @@ def tgv_solve(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04,
             MODES[mode], C.byref(p), _ptr(ui), _ptr(out), ls, C.byref(nls), nthreads)
     assert rc == 0, rc
     stats = [dict(depth=ls[i].depth, iters_run=ls[i].iters_run, active=ls[i].active,
-                  residual=ls[i].residual) for i in range(nls.value)]
+                  residual=ls[i].residual, energy=ls[i].energy) for i in range(nls.value)]
     return out, stats
 
 

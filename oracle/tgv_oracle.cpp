@@ -502,6 +502,36 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
             if (d > 0) return find(parent_key(nk, d));
             return -1;
         };
+        // FP64 primal energy of a level's state (the GPU library reports it per
+        // level; no counterpart in the reference): tot |u - med| + alpha1 |grad u - v|
+        // + alpha0 |e(v)|, forward differences to the in-memory neighbour (a
+        // missing one counts as the cube itself), e(v) in Voigt form with the
+        // off-diagonals halved and counted once.
+        auto energy_of = [&](const std::vector<uint32_t>& lv) -> double {
+            double e = 0.0;
+            for (uint32_t i : lv) {
+                const St<S>& c0 = st[i];
+                uint32_t tot = 0;
+                for (int k = 0; k < NB; ++k) tot += P.hists[size_t(i) * NB + k];
+                if (tot) e += double(tot) * std::fabs(double(c0.u) - double(dt[i].med));
+                double nu[3], nv[3][3];
+                for (int c = 0; c < 3; ++c) {
+                    const int32_t j = nb_of(i, 2 * c);
+                    const St<S>& t = j < 0 ? c0 : st[j];
+                    nu[c] = double(t.u);
+                    for (int k = 0; k < 3; ++k) nv[c][k] = double(t.v[k]);
+                }
+                const double u = c0.u, v0 = c0.v[0], v1 = c0.v[1], v2 = c0.v[2];
+                const double g0 = (nu[0] - u) - v0, g1 = (nu[1] - u) - v1, g2 = (nu[2] - u) - v2;
+                e += double(P.alpha1) * std::sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+                const double e0 = nv[0][0] - v0, e1 = nv[1][1] - v1, e2 = nv[2][2] - v2;
+                const double e3 = 0.5 * ((nv[1][0] - v0) + (nv[0][1] - v1));
+                const double e4 = 0.5 * ((nv[2][0] - v0) + (nv[0][2] - v2));
+                const double e5 = 0.5 * ((nv[2][1] - v1) + (nv[1][2] - v2));
+                e += double(P.alpha0) * std::sqrt(e0 * e0 + e1 * e1 + e2 * e2 + e3 * e3 + e4 * e4 + e5 * e5);
+            }
+            return e;
+        };
         std::vector<std::vector<uint32_t>> by_d(max_d + 1);
         for (int64_t i = 0; i < N; ++i) by_d[P.cubes[i].depth].push_back(uint32_t(i));
         for (int L = min_d; L <= max_d; ++L) {
@@ -550,6 +580,7 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
                 }
                 ls.iters_run = it_max;
             }
+            ls.energy = energy_of(all);
             if (lstats) lstats[nls] = ls;
             ++nls;
         }

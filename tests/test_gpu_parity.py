@@ -314,6 +314,25 @@ def test_wavefront_schedules_at_scale():
             ctx.set_schedule(mode, -1, -1)
 
 
+@pytest.mark.parametrize("mode", ["inmem", "oc"])
+def test_level_energy_matches_oracle(oracle_lib, mode):
+    """The FP64 per-level primal energy (tgvg_stats.energy) against the oracle's
+    FP64 sum over the same bit-identical state: equal to 1e-12 relative (only
+    the summation order differs)."""
+    rng = np.random.default_rng(23)
+    cubes = S.random_octree(rng, dmin=2, dmax=7, target=20000, shape="sphere")
+    hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.1)
+    leaves = S.split_leaves(len(cubes), 6, rng, cubes, aligned=True)
+    lv = None if mode == "inmem" else leaves
+    ref, rst = oracle_lib.tgv_solve(cubes, hists, lv, mode, 2.0, 1.0, 40, nthreads=8)
+    out, st = api.tgv_solve(cubes, hists, lv, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=40))
+    assert_state_equal(out, ref, "energy case")
+    want = [r["energy"] for r in rst]
+    assert st["depth"] == [r["depth"] for r in rst]
+    assert all(e > 0 for e in want)
+    np.testing.assert_allclose(st["energy"], want, rtol=1e-12)
+
+
 def test_tgv_stopping_rule(oracle_lib):
     """Per-level (per-leaf in OC and streaming) stop at relative residual <= tol.  A
     level that stops early has residual <= tol; the iteration counts and the

@@ -103,7 +103,7 @@ class Stats(C.Structure):
                 ("kt_depth", C.c_int32), ("kt_launches", C.c_int32), ("kt_active", C.c_int64),
                 ("kt_dual_ms", C.c_double), ("kt_primal_ms", C.c_double),
                 ("level_ms", C.c_double * MAX_LEVELS), ("schedule", C.c_int32 * MAX_LEVELS),
-                ("kt_fused", C.c_int32), ("reserved", C.c_int32)]
+                ("kt_fused", C.c_int32), ("reserved", C.c_int32), ("energy", C.c_double * MAX_LEVELS)]
 
     def as_dict(self):
         k = self.n_levels
@@ -114,7 +114,8 @@ class Stats(C.Structure):
                     setup_ms=self.setup_ms, iterate_ms=self.iterate_ms, total_ms=self.total_ms,
                     kt_depth=self.kt_depth, kt_launches=self.kt_launches, kt_active=self.kt_active,
                     kt_dual_ms=self.kt_dual_ms, kt_primal_ms=self.kt_primal_ms,
-                    level_ms=list(self.level_ms[:k]), schedule=list(self.schedule[:k]), kt_fused=self.kt_fused)
+                    level_ms=list(self.level_ms[:k]), schedule=list(self.schedule[:k]), kt_fused=self.kt_fused,
+                    energy=list(self.energy[:k]))
 
 
 P = C.c_void_p

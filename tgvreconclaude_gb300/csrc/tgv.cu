@@ -840,6 +840,44 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_cta(IterArgs a) {
     }
 }
 
+// Primal energy of one level's state in FP64 (no counterpart in the reference;
+// reported per level):  sum over the level's cubes of  tot |u - median|  +
+// alpha1 |grad u - v|  +  alpha0 |e(v)|, with the iteration's own operators:
+// forward differences along +x/+y/+z to the neighbour the sweeps use (a
+// missing neighbour counts as the cube itself) and e(v) in Voigt form with the
+// off-diagonal terms halved and counted once, as in the q ball.  Neighbour
+// values are the current state (u, v), whatever the semantics' border rule.
+template <int MODE>
+__global__ void k_energy(int o, int cnt, int npos, const int* __restrict__ nb, const float4* __restrict__ uv,
+                         const float2* __restrict__ dat, float alpha0, float alpha1, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    if (i < cnt) {
+        const int p = o + i;
+        const float4 s = uv[p];
+        const float2 D = dat[p];
+        if (D.y >= 0.0f) e += 4.0 * (double)D.y * fabs((double)s.x - (double)D.x);  // tot = 4 * (tau tot)
+        double nu[3], nv[3][3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int j = __ldg(nb + (size_t)(2 * c) * npos + p);
+            const float4 t = j < 0 ? s : uv[j & POS_MASK];
+            nu[c] = (double)t.x;
+            nv[c][0] = (double)t.y; nv[c][1] = (double)t.z; nv[c][2] = (double)t.w;
+        }
+        const double u = s.x, v0 = s.y, v1 = s.z, v2 = s.w;
+        const double g0 = (nu[0] - u) - v0, g1 = (nu[1] - u) - v1, g2 = (nu[2] - u) - v2;
+        e += (double)alpha1 * sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+        const double e0 = nv[0][0] - v0, e1 = nv[1][1] - v1, e2 = nv[2][2] - v2;
+        const double e3 = 0.5 * ((nv[1][0] - v0) + (nv[0][1] - v1));
+        const double e4 = 0.5 * ((nv[2][0] - v0) + (nv[0][2] - v2));
+        const double e5 = 0.5 * ((nv[2][1] - v1) + (nv[1][2] - v2));
+        e += (double)alpha0 * sqrt(e0 * e0 + e1 * e1 + e2 * e2 + e3 * e3 + e4 * e4 + e5 * e5);
+    }
+    for (int w = 16; w > 0; w >>= 1) e += __shfl_xor_sync(0xffffffffu, e, w);
+    if ((threadIdx.x & 31) == 0 && e != 0.0) atomicAdd(out, e);
+}
+
 // Stopping test after a residual iteration: relative fixed-point residual
 // (|x+ - x| + |y+ - y|) / (|x+| + |y+|) in FP64 per slot (sigma = tau).
 __global__ void k_check(int s0, int ns, double* __restrict__ acc, int* __restrict__ done, float tol, int iter,
@@ -2833,12 +2871,15 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         lv_it = reinterpret_cast<int*>(lvstat + TGVG_MAX_LEVELS * nslot);
     }
     std::vector<int> used(nlv, -1);
+    auto* lv_en = (double*)B(B_LVENERGY, 8ull * TGVG_MAX_LEVELS);
+    if (!lv_en) return TGVG_ERR_NOMEM;
 
     // Enqueue every level.  Device-only work: stopping flags and per-level
     // iteration counts / residuals stay on the device (copied per level into
     // lv_it / lv_res) and are read once after the loop, so the sequence can be
     // captured into a CUDA graph.
     auto enqueue = [&](bool capturing) -> int {
+        TGVG_CK(ctx, cudaMemsetAsync(lv_en, 0, 8ull * TGVG_MAX_LEVELS, ctx->stream));
         for (int k = 0; k < (int)levels.size(); ++k) {
             const Level& lvl = levels[k];
             const int Ld = lvl.d, o = lvl.o, cnt = lvl.cnt;
@@ -2893,6 +2934,13 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                     TGVG_CK(ctx, cudaMemcpyAsync(lv_res + k * nslot, resid, 8ull * nslot,
                                                  cudaMemcpyDeviceToDevice, ctx->stream));
                 }
+                if (mode == M_INMEM)
+                    k_energy<M_INMEM><<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, n, nb, uv, dat, prm->alpha0,
+                                                                                   prm->alpha1, lv_en + k);
+                else
+                    k_energy<M_STREAM><<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, n, nb, uv, dat,
+                                                                                    prm->alpha0, prm->alpha1, lv_en + k);
+                TGVG_LAUNCHED(ctx);
             }
         }
         return TGVG_OK;
@@ -2979,6 +3027,9 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         TGVG_CK(ctx, cudaMemcpyAsync(h_it.data(), lv_it, 4ull * nlv * nslot, cudaMemcpyDeviceToHost, ctx->stream));
         TGVG_CK(ctx, cudaMemcpyAsync(h_rs.data(), lv_res, 8ull * nlv * nslot, cudaMemcpyDeviceToHost, ctx->stream));
     }
+    double h_en[TGVG_MAX_LEVELS] = {};
+    if (nlv > 0)
+        TGVG_CK(ctx, cudaMemcpyAsync(h_en, lv_en, 8ull * nlv, cudaMemcpyDeviceToHost, ctx->stream));
     int h_err = 0;
     TGVG_CK(ctx, cudaMemcpyAsync(&h_err, flags + 6, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -2990,6 +3041,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         const Level& lvl = levels[k];
         st.n_levels = k + 1;
         st.schedule[k] = used[k];
+        st.energy[k] = h_en[k];
         st.depth[k] = lvl.d;
         st.active[k] = lvl.cnt;
         if (stop) {
