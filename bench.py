@@ -314,20 +314,26 @@ def surface_eval(args, w, out_t):
     """Surface extraction (extract_surface with has_data and normals) of the
     solved state through the host-buffer C ABI call, and the CPU oracle on a
     bounded contiguous Morton slice of the same input."""
+    import torch
     from tgvreconclaude_gb300 import api, formats as F
     n = len(w.cubes)
-    state = out_t.cpu().numpy().view(F.STATE_DTYPE).reshape(n).copy()
-    has = (w.hists.sum(1) > 0).astype(np.uint8)
+    # inputs in pinned host memory, as for the solver's e2e
+    state = torch.empty(out_t.shape, dtype=out_t.dtype, pin_memory=True)
+    state.copy_(out_t)
+    state = state.numpy().view(F.STATE_DTYPE).reshape(n)
+    has = torch.from_numpy((w.hists.sum(1) > 0).astype(np.uint8)).pin_memory().numpy()
+    cubes = torch.from_numpy(w.cubes.view(np.int32).reshape(n, 4).copy()).pin_memory().numpy()
+    cubes = cubes.view(F.CUBE_DTYPE).reshape(n)
     o, r = np.float32(w.cfg["origin"]), float(w.cfg["r_root"])
-    api.extract_surface(w.cubes[:1000], state[:1000], o, r, has_data=has[:1000], normals=True)  # warm-up
+    api.extract_surface(cubes[:1000], state[:1000], o, r, has_data=has[:1000], normals=True)  # warm-up
     ts = []
     for _ in range(3):
         t0 = time.perf_counter()
-        v, f, _ = api.extract_surface(w.cubes, state, o, r, has_data=has, normals=True)
+        v, f, _ = api.extract_surface(cubes, state, o, r, has_data=has, normals=True)
         ts.append(time.perf_counter() - t0)
     t = float(np.median(ts))
     res = {"cubes": n, "vertices": int(len(v)), "triangles": int(len(f)), "ms_e2e": 1e3 * t,
-           "cubes_per_s_e2e": n / t, "what": "extract_surface + compute_normals, host arrays in and out"}
+           "cubes_per_s_e2e": n / t, "what": "extract_surface + compute_normals, inputs in pinned host memory, mesh returned in host arrays"}
     if not args.skip_cpu:
         sys.path.insert(0, os.path.join(HERE, "oracle"))
         import oracle as O
