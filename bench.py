@@ -426,7 +426,7 @@ def warm_start_eval(args):
                          ref_leaf_iters=st["leaf_iters"],
                          capped_levels=[sum(i >= 6000 for i in r) for r in (zero.iters, warm.iters, st["iters_run"])]))
     med = lambda k: float(np.median([r[k] for r in recs]))
-    return {"tol": 1e-4, "max_iters_per_level": 6000, "scenes": len(recs),
+    return {"tol": 1e-4, "max_iters_per_level": 6000, "scenes": len(recs), "graphs": "off (direct launches)",
             "scene": "16 cameras at 320x240, torus (depth 7) / three objects (depth 8), held-out seeds 1000+",
             "median_zero_ms": med("zero_ms"), "median_warm_ms": med("warm_ms"), "median_ref_ms": med("ref_ms"),
             "time_ratio_zero_over_warm": float(np.median([r["zero_ms"] / r["warm_ms"] for r in recs])),
