@@ -5,7 +5,7 @@ reference's histogram and TGV algorithms (oracle/tgv_oracle.cpp); ``libref`` is
 the reference's own src/*.cpp compiled unmodified with the project-written
 Eigen/TBB shims (oracle/Makefile, built only where the reference checkout
 exists).  Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this module, as the checker or the timed CPU baseline.
+``bench.py`` import this module, to check results or as the timed CPU baseline.
 """
 from __future__ import annotations
 

@@ -3,7 +3,7 @@
 //
 // TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
 // baseline leg of bench.py load this library (oracle/_build/liboracle.so), and
-// only as the checker or the timed CPU baseline; the product never calls it.
+// only to check results or as the timed CPU baseline; the product never calls it.
 //
 // Pinning: the float instantiation at NBINS=8 is checked bit-for-bit against
 // the reference's own src/histogram.cpp and src/tgv.cpp compiled unmodified
