@@ -344,6 +344,7 @@ struct IterArgs {
     int pf;               // per-launch schedules: L2 prefetch of the warp's next group (0 = off)
     int swap;             // per-launch schedules: dual sweep in reverse order, primal forward
     int band;             // per-launch schedules: warps stride over the whole unit (grid-stride band)
+    int lend;             // end of the level's positions; cubes at lend and beyond are deeper
 };
 
 // Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
@@ -499,24 +500,27 @@ __device__ __forceinline__ void primal_load_own(const IterArgs& a, int p, Primal
     L.j5 = __ldg(a.nb + 5 * a.npos + p);
 }
 
-// ... and the p/q of its -x/-y/-z neighbours.
+// ... and the p/q of its -x/-y/-z neighbours.  A neighbour found by code can be
+// a deeper cube (an octant-0 descendant shares the code, tgv.cpp:97-109,369-370).
+// Levels run coarse to fine, so a deeper cube's p/q still hold their initial
+// zeros while this level runs: such a neighbour reads as 0 without a load.
 template <int MODE, bool CG>
 __device__ __forceinline__ void primal_load_gather(const IterArgs& a, PrimalLd& L) {
     const int j1 = L.j1, j3 = L.j3, j5 = L.j5;
     L.gp10 = L.gq10 = L.gq13 = L.gq14 = 0.f;
     L.gp31 = L.gq31 = L.gq33 = L.gq35 = 0.f;
     L.gp52 = L.gq52 = L.gq54 = L.gq55 = 0.f;
-    if (j1 >= 0 && !(MODE == M_STREAM && (j1 & BORDER))) {
+    if (j1 >= 0 && !(MODE == M_STREAM && (j1 & BORDER)) && (j1 & POS_MASK) < a.lend) {
         const int j = j1 & POS_MASK;
         const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
         L.gp10 = a4.x; L.gq10 = a4.w; L.gq13 = b4.z; L.gq14 = b4.w;
     }
-    if (j3 >= 0 && !(MODE == M_STREAM && (j3 & BORDER))) {
+    if (j3 >= 0 && !(MODE == M_STREAM && (j3 & BORDER)) && (j3 & POS_MASK) < a.lend) {
         const int j = j3 & POS_MASK;
         const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
         L.gp31 = a4.y; L.gq31 = b4.x; L.gq33 = b4.z; L.gq35 = ld1<CG>(a.Q1 + j);
     }
-    if (j5 >= 0 && !(MODE == M_STREAM && (j5 & BORDER))) {
+    if (j5 >= 0 && !(MODE == M_STREAM && (j5 & BORDER)) && (j5 & POS_MASK) < a.lend) {
         const int j = j5 & POS_MASK;
         const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
         L.gp52 = a4.z; L.gq52 = b4.y; L.gq54 = b4.w; L.gq55 = ld1<CG>(a.Q1 + j);
@@ -2910,7 +2914,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
             for (const Unit& u : lvl.us) {
                 IterArgs a;
                 std::memset(&a, 0, sizeof(a));
-                a.o = u.o; a.n = u.n; a.npos = n;
+                a.o = u.o; a.n = u.n; a.npos = n; a.lend = o + cnt;
                 a.nb = nb; a.uv = uv; a.bar = bar; a.P4 = P4; a.Q4 = Q4; a.Q1 = Q1; a.dat = dat; a.snap = snap;
                 a.lid = lid; a.acc = acc; a.done = done; a.slot0 = u.slot;
                 a.alpha0 = prm->alpha0; a.alpha1 = prm->alpha1;
