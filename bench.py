@@ -463,6 +463,11 @@ def run_ours(args):
     mode = "stream" if cfg["chunks"] > 1 else "inmem"
     leaves = w.leaves if mode == "stream" else None
     stream = torch.cuda.ExternalStream(ctx.stream)
+    # fixed schedules per size class (floor(log2 cubes)) instead of the online
+    # autotuner: a profiler's serialised launches would skew the tuner's timings
+    for item in filter(None, args.schedules.split(",")):
+        cls, sched = (int(v) for v in item.split(":"))
+        ctx.set_schedule(mode, cls, sched)
 
     # warm-up: the first step autotunes every level's schedule (direct launches);
     # with per-launch timing on, the third captures the level loop into a CUDA
@@ -573,6 +578,7 @@ def run_ours(args):
                        "semantics": "tgv_minimize" if mode == "inmem" else "tgv_minimize_streaming (batched)",
                        "chunks": len(w.leaves), "levels": {int(k): int(v) for k, v in enumerate(depth_hist) if v},
                        "l2": "inputs larger than L2 (about 100 B of state per cube)",
+                       "schedules": args.schedules or "autotuned",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "fp64_check": f64, "histograms": hs, "surface": surf,
             "stages_1_3": s13,
@@ -619,6 +625,7 @@ def main():
     ap.add_argument("--warm-seeds", type=int, default=6)
     ap.add_argument("--max-cubes", type=int, default=0, help="truncate the workload (profiling runs)")
     ap.add_argument("--cache", default="", help="load the workload from / save it to this .npz (profiling runs)")
+    ap.add_argument("--schedules", default="", help="fix schedules, e.g. 17:15,21:14 (size class:schedule; profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
