@@ -26,15 +26,31 @@ from tgvreconclaude_gb300.formats import (  # noqa: E402
 
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
-REF_DIR = os.environ.get("TGV_REFERENCE_DIR", "/root/reference")
+_REF_DIR = None
+
+
+def ref_dir() -> str:
+    """The reference checkout: $TGV_REFERENCE_DIR, else the build recipe's
+    default (oracle/Makefile REF_DIR).  It exists only where the reference was
+    checked out; nothing that runs on the GPU needs it."""
+    global _REF_DIR
+    if _REF_DIR is None:
+        d = os.environ.get("TGV_REFERENCE_DIR", "")
+        if not d:
+            r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref-dir"],
+                               capture_output=True, text=True)
+            d = r.stdout.strip()
+        _REF_DIR = d
+    return _REF_DIR
 
 
 def build(ref: bool = False) -> None:
     """Compile the oracle (and, when asked and the reference exists, libref)."""
     targets = ["all"]
-    if ref and os.path.isdir(os.path.join(REF_DIR, "src")):
+    rd = ref_dir()
+    if ref and rd and os.path.isdir(os.path.join(rd, "src")):
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, f"REF_DIR={REF_DIR}", f"-j{os.cpu_count() or 4}"]
+    subprocess.run(["make", "-s", "-C", HERE, f"REF_DIR={rd}", f"-j{os.cpu_count() or 4}"]
                    + targets, check=True)
 
 
@@ -84,7 +100,8 @@ def lib():
 
 
 def ref_available() -> bool:
-    return os.path.exists(REF_SO) or os.path.isdir(os.path.join(REF_DIR, "src"))
+    rd = ref_dir()
+    return os.path.exists(REF_SO) or bool(rd and os.path.isdir(os.path.join(rd, "src")))
 
 
 def ref():
@@ -180,10 +197,14 @@ INITS = {"median": 0, "zero": 1, "given": 2}
 
 
 def tgv_solve(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04, iters=200,
-              init="median", u_init=None, tol=0.0, check_every=10, fp64=False, nthreads=1, keep_init_u=False):
+              init="median", u_init=None, tol=0.0, check_every=10, fp64=False, nthreads=1, keep_init_u=False,
+              level_init=None):
     """Oracle solve.  Returns (state, level_stats).  State is a STATE_DTYPE array
     (float) or an (n, 13) float64 array when fp64.  keep_init_u: levels keep
-    their initial u and copy only v from the parent (warm / zero start)."""
+    their initial u and copy only v from the parent (warm / zero start).
+    level_init (STATE_DTYPE, float solve only): every cube starts its level from
+    this whole state (u, v, p, q) instead of the parent copy; until its level
+    starts it holds the state `init` gives."""
     cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
     hists = np.ascontiguousarray(hists, np.uint32)
     n = len(cubes)
@@ -199,6 +220,16 @@ def tgv_solve(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04,
     ui = None if u_init is None else np.ascontiguousarray(u_init, np.float32)
     ls = (LevelStats * 24)()
     nls = C.c_int()
+    if level_init is not None:
+        assert not fp64
+        li = np.ascontiguousarray(level_init, STATE_DTYPE)
+        out = np.zeros(n, STATE_DTYPE)
+        rc = lib().orc_tgv_solve_level_init(_ptr(cubes), _ptr(hists), C.c_int64(n), nbins, _ptr(leaves),
+                                            len(leaves), MODES[mode], C.byref(p), _ptr(ui), _ptr(li), _ptr(out),
+                                            ls, C.byref(nls), nthreads)
+        assert rc == 0, rc
+        return out, [dict(depth=ls[i].depth, iters_run=ls[i].iters_run, active=ls[i].active,
+                          residual=ls[i].residual, energy=ls[i].energy) for i in range(nls.value)]
     if fp64:
         out = np.zeros((n, 13), np.float64)
         fn = lib().orc_tgv_solve_f64
@@ -211,6 +242,15 @@ def tgv_solve(cubes, hists, leaves=None, mode="inmem", alpha0=0.02, alpha1=0.04,
     stats = [dict(depth=ls[i].depth, iters_run=ls[i].iters_run, active=ls[i].active,
                   residual=ls[i].residual, energy=ls[i].energy) for i in range(nls.value)]
     return out, stats
+
+
+def neighbour_table(cubes):
+    """(n, 6) int32: the in-memory neighbour of every cube per face (+x, -x, +y,
+    -y, +z, -z), -1 where none (the reference's neighbor_idx_ctf)."""
+    cubes = np.ascontiguousarray(cubes, CUBE_DTYPE)
+    nb = np.zeros((len(cubes), 6), np.int32)
+    lib().orc_neighbour_table(_ptr(cubes), C.c_int64(len(cubes)), _ptr(nb))
+    return nb
 
 
 def stream_init(cubes, hists):

@@ -439,6 +439,11 @@ struct Problem {
     int only_level = -1;
     const State* state_in = nullptr;
     int keep_init_u = 0;  // extension: parent init copies only v (warm / zero start per level)
+    // Extension (warm start of the whole primal-dual state): when set, every
+    // cube takes level_init's (u, v, p, q) at its own level's start, in place of
+    // the parent copy and the zeroing of p and q; until then it holds the
+    // initial state `init` gives, like every cube of the plain solve.
+    const State* level_init = nullptr;
 };
 
 // Reference binary search over the Morton-sorted cube array: returns the first
@@ -451,6 +456,13 @@ static uint32_t file_lookup(const std::vector<uint64_t>& keys, uint64_t k) {
         if (keys[mid] < k) lo = mid + 1; else hi = mid;
     }
     return 0xffffffffu;
+}
+
+template <typename S>
+static void set_state(St<S>& d, const State& s) {
+    d.u = S(s.u);
+    for (int c = 0; c < 3; ++c) { d.v[c] = S(s.v[c]); d.p[c] = S(s.p[c]); }
+    for (int c = 0; c < 6; ++c) d.q[c] = S(s.q[c]);
 }
 
 template <typename S, int NB>
@@ -537,7 +549,12 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
         for (int L = min_d; L <= max_d; ++L) {
             const auto& all = by_d[L];
             if (all.empty()) continue;
-            if (L > min_d) {  // parent copy (tgv.cpp:391-409)
+            if (P.level_init) {  // whole given state at the level's start
+                for (uint32_t i : all) {
+                    set_state(st[i], P.level_init[i]);
+                    ub[i] = st[i].u; vbx[i] = st[i].v[0]; vby[i] = st[i].v[1]; vbz[i] = st[i].v[2];
+                }
+            } else if (L > min_d) {  // parent copy (tgv.cpp:391-409)
                 for (uint32_t i : all) {
                     int32_t pi = find(parent_key(keys[i], L));
                     if (pi >= 0) {
@@ -595,7 +612,14 @@ static int solve(const Problem<S, NB>& P, St<S>* out, LevelStats* lstats, int* n
         };
         for (int L = min_d; L <= max_d; ++L) {
             if (P.only_level >= 0 && L != P.only_level) continue;
-            if (L > min_d) {  // parent init, leaf by leaf (tgv.cpp:878-934)
+            if (P.level_init) {  // whole given state at the level's start, leaf by leaf
+                for (int l = 0; l < P.nleaf; ++l) {
+                    uint32_t f0, nl;
+                    if (!leaf_range(l, f0, nl)) continue;
+                    for (uint32_t li = 0; li < nl; ++li)
+                        if (P.cubes[f0 + li].depth == L) set_state(st[f0 + li], P.level_init[f0 + li]);
+                }
+            } else if (L > min_d) {  // parent init, leaf by leaf (tgv.cpp:878-934)
                 for (int l = 0; l < P.nleaf; ++l) {
                     uint32_t f0, nl;
                     if (!leaf_range(l, f0, nl)) continue;
@@ -1050,18 +1074,20 @@ int orc_project(const orc::Camera* cam, float px, float py, float pz, float r_c,
 static int solve_f32(const orc::Cube* cubes, const uint32_t* hists, int64_t n, int nbins,
                      const orc::Leaf* leaves, int nleaf, int mode, const orc_params* p,
                      const float* u_init, orc::State* out, orc::LevelStats* ls, int* nls,
-                     int nthreads) {
+                     int nthreads, const orc::State* level_init = nullptr) {
     std::vector<orc::St<float>> s(static_cast<size_t>(n));
     int rc;
     if (nbins == 8) {
         orc::Problem<float, 8> P{cubes, n, hists, leaves, nleaf, mode, p->alpha0, p->alpha1, p->iters,
                                  p->init, u_init, p->tol, p->check_every, nthreads};
         P.keep_init_u = p->keep_init_u;
+        P.level_init = level_init;
         rc = orc::solve<float, 8>(P, s.data(), ls, nls);
     } else if (nbins == 10) {
         orc::Problem<float, 10> P{cubes, n, hists, leaves, nleaf, mode, p->alpha0, p->alpha1, p->iters,
                                   p->init, u_init, p->tol, p->check_every, nthreads};
         P.keep_init_u = p->keep_init_u;
+        P.level_init = level_init;
         rc = orc::solve<float, 10>(P, s.data(), ls, nls);
     } else {
         return -1;
@@ -1078,6 +1104,18 @@ int orc_tgv_solve(const orc::Cube* cubes, const uint32_t* hists, int64_t n, int 
                   const float* u_init, orc::State* out, orc::LevelStats* ls, int* nls,
                   int nthreads) {
     return solve_f32(cubes, hists, n, nbins, leaves, nleaf, mode, p, u_init, out, ls, nls, nthreads);
+}
+
+// Float solve in which every cube starts its level from the whole given state
+// (u, v, p, q; TGVCube records) instead of the parent copy; the initial state
+// of not-yet-run cubes comes from p->init as in the plain solve.  Warm start of
+// the whole primal-dual state; no counterpart in the reference.
+int orc_tgv_solve_level_init(const orc::Cube* cubes, const uint32_t* hists, int64_t n, int nbins,
+                             const orc::Leaf* leaves, int nleaf, int mode, const orc_params* p,
+                             const float* u_init, const orc::State* level_init, orc::State* out,
+                             orc::LevelStats* ls, int* nls, int nthreads) {
+    return solve_f32(cubes, hists, n, nbins, leaves, nleaf, mode, p, u_init, out, ls, nls, nthreads,
+                     level_init);
 }
 
 // FP64 oracle of the same solver.  out: n * 13 doubles (u, v[3], p[3], q[6]).
@@ -1330,4 +1368,35 @@ extern "C" int64_t orc_balance_cubes(const orc::Cube* in, int64_t n, float r_roo
     orc::balance_cubes(in, n, r_root, cs);
     if (out && cap >= int64_t(cs.size())) std::memcpy(out, cs.data(), cs.size() * sizeof(orc::Cube));
     return int64_t(cs.size());
+}
+
+extern "C" {
+// In-memory neighbour table of every cube (neighbor_idx_ctf over the code map
+// code -> largest index, tgv.cpp:97-109, 367-370): nb[6 i + f] = the index of
+// cube i's face-f neighbour, else -1 (faces +x, -x, +y, -y, +z, -z).
+void orc_neighbour_table(const orc::Cube* cubes, int64_t n, int32_t* nb) {
+    std::unordered_map<uint64_t, uint32_t> cmap;
+    cmap.reserve(size_t(n) * 2);
+    std::vector<uint64_t> keys(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        keys[i] = orc::key_of(cubes[i].hi, cubes[i].lo);
+        cmap[keys[i]] = uint32_t(i);
+    }
+    auto find = [&](uint64_t k) -> int32_t {
+        auto it = cmap.find(k);
+        return it == cmap.end() ? -1 : int32_t(it->second);
+    };
+    for (int64_t i = 0; i < n; ++i) {
+        const int d = cubes[i].depth;
+        for (int f = 0; f < 6; ++f) {
+            int32_t r = -1;
+            const uint64_t nk = orc::face_key(keys[i], f, d);
+            if (!orc::is_none(nk)) {
+                r = find(nk);
+                if (r < 0 && d > 0) r = find(orc::parent_key(nk, d));
+            }
+            nb[size_t(i) * 6 + f] = r;
+        }
+    }
+}
 }

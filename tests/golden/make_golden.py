@@ -3,9 +3,9 @@
 Runs the reference's own src/histogram.cpp, src/tgv.cpp and src/marching_cubes.cpp (compiled unmodified
 into oracle/_ref/libref.so by oracle/Makefile, with the project-written
 Eigen/TBB shims) on seeded synthetic inputs and stores inputs + outputs as
-compressed .npz files.  Needs the reference checkout (TGV_REFERENCE_DIR,
-default /root/reference); the fixtures it writes are committed so the tests can
-run where the reference is absent.
+compressed .npz files.  Needs the reference checkout ($TGV_REFERENCE_DIR, else
+the REF_DIR default of oracle/Makefile); the fixtures it writes are committed
+so the tests can run where the reference is absent.
 
     python tests/golden/make_golden.py            # histogram and TGV fixtures, then
     python tests/golden/make_golden.py --mesh     # the surface fixtures (read tgv_balanced.npz)

@@ -13,10 +13,12 @@ import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DROPIN = os.path.join(REPO, "tgvreconclaude_gb300", "dropin")
-REF_DIR = os.environ.get("TGV_REFERENCE_DIR", "/root/reference")
+import oracle  # noqa: E402  (tests/conftest.py puts oracle/ on the path)
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF_DIR, "tests")),
-                                reason="reference checkout absent")
+REF_DIR = oracle.ref_dir()
+
+pytestmark = pytest.mark.skipif(not REF_DIR or not os.path.isdir(os.path.join(REF_DIR, "tests")),
+                                reason="reference checkout absent (set TGV_REFERENCE_DIR)")
 
 
 def test_dropin_links_reference_tests():

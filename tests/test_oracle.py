@@ -181,3 +181,81 @@ def test_kat_stage5_project_and_plane(oracle_lib):
     c = F.make_cubes([int(F.morton_encode(np.uint32(4 << 17), np.uint32(4 << 17), np.uint32(8 << 17)))], 4, 1 / 16)
     h = oracle_lib.compute_histograms(c, [plane], (-0.5, -0.5, 4.0), 1.0)
     assert h.sum() > 0 and h[0, :4].sum() > h[0, 4:].sum()
+
+
+# ---- whole-state warm start (level_init): an extension with no counterpart in the
+# reference, pinned here to the reference's own level start (tgv.cpp:391-409).
+
+def _level_start_records(cubes, hists, final):
+    """The state each cube has when its level starts in the plain solve:
+    u and v of the cube that the parent-code lookup returns (the largest index
+    with that code; its state is final when it is coarser, initial otherwise),
+    p = q = 0; the cube's own initial state where no such cube exists or on the
+    coarsest level."""
+    keys = F.cube_keys(cubes).astype(np.uint64)
+    d = cubes["depth"].astype(np.int64)
+    init = np.zeros(len(cubes), F.STATE_DTYPE)
+    import oracle
+    init["u"] = oracle.stream_init(cubes, hists)["u"]
+    last = {}
+    for i, k in enumerate(keys.tolist()):
+        last[k] = i
+    rec = init.copy()
+    dmin = int(d.min())
+    for i in range(len(cubes)):
+        L = int(d[i])
+        if L == dmin:
+            continue
+        sh = 3 * (21 - (L - 1))
+        pk = int(keys[i]) >> sh << sh
+        j = last.get(pk, -1)
+        if j < 0:
+            continue
+        src = final[j] if d[j] < L else init[j]
+        rec["u"][i] = src["u"]
+        rec["v"][i] = src["v"]
+    return rec
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_level_init_reproduces_the_reference_level_start(oracle_lib, seed):
+    """Seeding every level with the records the reference's parent copy would
+    produce gives the plain solve bit for bit, in in-memory semantics."""
+    rng = np.random.default_rng(70 + seed)
+    cubes = S.random_octree(rng, dmin=1 + seed, dmax=4 + seed, target=2500, shape=["sphere", "plane", "random"][seed])
+    hists = S.random_histograms(rng, len(cubes), nbins=8 if seed % 2 == 0 else 10)
+    plain, pst = oracle_lib.tgv_solve(cubes, hists, None, "inmem", 2.0, 1.0, 25)
+    rec = _level_start_records(cubes, hists, plain)
+    out, ost = oracle_lib.tgv_solve(cubes, hists, None, "inmem", 2.0, 1.0, 25, level_init=rec)
+    assert out.tobytes() == plain.tobytes()
+    assert [s["iters_run"] for s in ost] == [s["iters_run"] for s in pst]
+
+
+def test_level_init_zero_records_on_one_level(oracle_lib):
+    """All-zero records on a one-level octree are the zero initialisation."""
+    rng = np.random.default_rng(3)
+    cubes = S.random_octree(rng, dmin=4, dmax=4, target=1500)
+    hists = S.random_histograms(rng, len(cubes))
+    z = np.zeros(len(cubes), F.STATE_DTYPE)
+    a, _ = oracle_lib.tgv_solve(cubes, hists, None, "inmem", 2.0, 1.0, 30, init="zero")
+    b, _ = oracle_lib.tgv_solve(cubes, hists, None, "inmem", 2.0, 1.0, 30, level_init=z)
+    assert a.tobytes() == b.tobytes()
+
+
+def test_neighbour_table_on_a_uniform_grid(oracle_lib):
+    """Every cell of a full 4^3 grid at depth 2 has its face-adjacent cells as
+    neighbours and -1 across the domain boundary."""
+    g = np.arange(4, dtype=np.uint32)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    sh = F.MAX_DEPTH - 2
+    k = F.morton_encode(X.ravel() << sh, Y.ravel() << sh, Z.ravel() << sh)
+    o = np.argsort(k)
+    cubes = F.make_cubes(k[o], np.full(len(k), 2, np.int32), np.full(len(k), 0.25, np.float32))
+    nb = oracle_lib.neighbour_table(cubes)
+    xyz = np.stack([X.ravel()[o], Y.ravel()[o], Z.ravel()[o]], 1)
+    pos = {tuple(p): i for i, p in enumerate(xyz.tolist())}
+    for i, p in enumerate(xyz.tolist()):
+        for f in range(6):
+            q = list(p)
+            q[f // 2] += 1 if f % 2 == 0 else -1
+            assert nb[i, f] == pos.get(tuple(q), -1)
