@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define TGVG_ABI_VERSION 3
+#define TGVG_ABI_VERSION 4
 
 /* ---- status codes -------------------------------------------------------- */
 #define TGVG_OK             0
@@ -92,6 +92,7 @@ typedef struct tgvg_params {
 #define TGVG_INIT_MEDIAN 0   /* u = median_indicator (reference, tgv.cpp:372-373) */
 #define TGVG_INIT_ZERO   1   /* u = 0 ("plain solver from a zero start")          */
 #define TGVG_INIT_GIVEN  2   /* u = caller array (learned warm start)             */
+#define TGVG_INIT_STATE  3   /* whole-state warm start: tgvg_tgv_minimize_state   */
 
 #define TGVG_MODE_INMEM  0   /* tgv_minimize           (tgv.cpp:356-419) */
 #define TGVG_MODE_OC     1   /* tgv_minimize_oc        (tgv.cpp:423-511) */
@@ -282,6 +283,26 @@ int tgvg_tgv_minimize_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_
                           int64_t n, int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf,
                           int32_t mode, const tgvg_params* params, const float* d_u_init,
                           tgvg_state* d_out, tgvg_stats* stats);
+
+/* Whole-state warm start (no counterpart in the reference; params->init must be
+ * TGVG_INIT_STATE).  Every cube starts its own level from init_state[i] (u, v,
+ * p and q of a TGVCube record) in place of the reference's parent copy of u, v
+ * and zeroing of p, q (tgv.cpp:391-409, 878-934); until its level starts it
+ * holds the reference's initial state (u = median indicator, v = p = q = 0),
+ * so coarser levels that read it as a deeper neighbour see exactly what the
+ * plain solve shows them, and every level solves the reference's problem.
+ * Records equal to what the parent copy would give reproduce the plain solve;
+ * all-zero records are a zero start of every level.  keep_init_u is ignored.
+ * Host arrays (the _dev form: device arrays, leaves on the host), otherwise as
+ * tgvg_tgv_minimize. */
+int tgvg_tgv_minimize_state(tgvg_ctx* ctx, const tgvg_cube* cubes, const uint32_t* hists, int64_t n,
+                            int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, int32_t mode,
+                            const tgvg_params* params, const tgvg_state* init_state, tgvg_state* out,
+                            tgvg_stats* stats);
+int tgvg_tgv_minimize_state_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists, int64_t n,
+                                int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, int32_t mode,
+                                const tgvg_params* params, const tgvg_state* d_init_state, tgvg_state* d_out,
+                                tgvg_stats* stats);
 
 /* tgv_minimize_streaming (reference src/tgv.hpp:57-64, tgv.cpp:802-1070): TGV1
  * cube file, TGVH histogram file (8 bins) and TGVT treetop file in, TGVS state

@@ -30,7 +30,7 @@ def test_header_declarations_are_all_exported():
 
 def test_abi_version_and_errors():
     lib = N.lib()
-    assert lib.tgvg_abi_version() == 3
+    assert lib.tgvg_abi_version() == 4
     assert lib.tgvg_strerror(-4).decode() == "cubes are not sorted by Morton code"
     assert lib.tgvg_strerror(-9).decode() == "treetop leaves overlap"
 

@@ -142,6 +142,9 @@ _SIGS = {
                                    C.c_int),
     "tgvg_tgv_minimize": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P], C.c_int),
     "tgvg_tgv_minimize_dev": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P], C.c_int),
+    "tgvg_tgv_minimize_state": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P], C.c_int),
+    "tgvg_tgv_minimize_state_dev": ([P, P, P, C.c_int64, C.c_int32, P, C.c_int32, C.c_int32, P, P, P, P],
+                                    C.c_int),
     "tgvg_tgv_minimize_streaming": ([P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, P, P], C.c_int),
     "tgvg_mlp_create": ([P, C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)], C.c_int),
     "tgvg_mlp_destroy": ([P], C.c_int),

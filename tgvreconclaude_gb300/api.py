@@ -345,21 +345,25 @@ class TGVParams:
     alpha0: float = 0.02
     alpha1: float = 0.04
     iters: int = 200
-    init: str = "median"       # "median" (reference), "zero", "given"
+    init: str = "median"       # "median" (reference), "zero", "given", "state" (whole-state start per level)
     tol: float = 0.0           # relative residual stop; 0 = fixed iteration count
     check_every: int = 10
     keep_init_u: bool = False  # True: every level keeps its initial u (warm / zero start), copies only v
 
     def struct(self) -> N.Params:
-        return N.Params(self.alpha0, self.alpha1, self.iters, {"median": 0, "zero": 1, "given": 2}[self.init],
+        return N.Params(self.alpha0, self.alpha1, self.iters,
+                        {"median": 0, "zero": 1, "given": 2, "state": 3}[self.init],
                         self.tol, self.check_every, int(self.keep_init_u))
 
 
 MODES = {"inmem": 0, "oc": 1, "stream": 2}
 
 
-def tgv_solve(cubes, hists, leaves=None, mode="inmem", params: TGVParams | None = None, u_init=None):
-    """Generic solve over host arrays -> (state (n,) STATE_DTYPE, stats dict)."""
+def tgv_solve(cubes, hists, leaves=None, mode="inmem", params: TGVParams | None = None, u_init=None,
+              state_init=None):
+    """Generic solve over host arrays -> (state (n,) STATE_DTYPE, stats dict).
+    state_init (STATE_DTYPE): whole-state warm start, every cube starts its
+    level from its record (params.init is taken as "state")."""
     ctx = context()
     params = params or TGVParams()
     cubes = np.ascontiguousarray(cubes, F.CUBE_DTYPE)
@@ -370,6 +374,13 @@ def tgv_solve(cubes, hists, leaves=None, mode="inmem", params: TGVParams | None 
     lv = None if leaves is None else np.ascontiguousarray(leaves, F.LEAF_DTYPE)
     ui = None if u_init is None else np.ascontiguousarray(u_init, np.float32)
     st = N.Stats()
+    if state_init is not None:
+        si = np.ascontiguousarray(state_init, F.STATE_DTYPE)
+        prm = TGVParams(**{**params.__dict__, "init": "state"}).struct()
+        ctx.check(ctx.lib.tgvg_tgv_minimize_state(ctx.h, _p(cubes), _p(hists), n, nbins, _p(lv),
+                                                  0 if lv is None else len(lv), MODES[mode], C.byref(prm), _p(si),
+                                                  _p(out), C.byref(st)), "tgv_minimize_state")
+        return out, st.as_dict()
     prm = params.struct()
     ctx.check(ctx.lib.tgvg_tgv_minimize(ctx.h, _p(cubes), _p(hists), n, nbins, _p(lv),
                                         0 if lv is None else len(lv), MODES[mode], C.byref(prm), _p(ui), _p(out),
@@ -400,15 +411,23 @@ def tgv_minimize_streaming(balanced_cube_path, hist_path, treetop_path, origin, 
 
 
 def tgv_solve_device(cubes_t, hists_t, out_t, leaves=None, mode="inmem", params: TGVParams | None = None,
-                     u_init_t=None):
+                     u_init_t=None, state_init_t=None):
     """Device-resident solve: torch CUDA tensors in and out (cubes (n,4) int32
-    view of the records, hists (n,nbins) int32/uint32, out (n,13) float32)."""
+    view of the records, hists (n,nbins) int32/uint32, out (n,13) float32).
+    state_init_t ((n,13) float32): whole-state warm start."""
     ctx = context()
     params = params or TGVParams()
     n = cubes_t.shape[0]
     nbins = hists_t.shape[1]
     lv = None if leaves is None else np.ascontiguousarray(leaves, F.LEAF_DTYPE)
     st = N.Stats()
+    if state_init_t is not None:
+        prm = TGVParams(**{**params.__dict__, "init": "state"}).struct()
+        ctx.check(ctx.lib.tgvg_tgv_minimize_state_dev(ctx.h, cubes_t.data_ptr(), hists_t.data_ptr(), n, nbins,
+                                                      _p(lv), 0 if lv is None else len(lv), MODES[mode],
+                                                      C.byref(prm), state_init_t.data_ptr(), out_t.data_ptr(),
+                                                      C.byref(st)), "tgv_minimize_state_dev")
+        return st.as_dict()
     prm = params.struct()
     ctx.check(ctx.lib.tgvg_tgv_minimize_dev(ctx.h, cubes_t.data_ptr(), hists_t.data_ptr(), n, nbins, _p(lv),
                                             0 if lv is None else len(lv), MODES[mode], C.byref(prm),

@@ -228,10 +228,20 @@ extern "C" int tgvg_tgv_minimize_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, co
                                d_out, stats);
 }
 
+extern "C" int tgvg_tgv_minimize_state_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists,
+                                           int64_t n, int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf,
+                                           int32_t mode, const tgvg_params* params,
+                                           const tgvg_state* d_init_state, tgvg_state* d_out, tgvg_stats* stats) {
+    if (!ctx || !params || params->init != TGVG_INIT_STATE) return TGVG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return tgvg::tgv_solve_dev(ctx, d_cubes, d_hists, n, nbins, leaves, nleaf, mode, params, nullptr, d_out, stats,
+                               d_init_state);
+}
+
 static int minimize_host(tgvg_ctx* ctx, const tgvg_cube* cubes, const uint32_t* hists, int64_t n,
                          int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, int32_t mode,
                          const tgvg_params* params, const float* u_init, tgvg_state* out,
-                         tgvg_stats* stats) {
+                         tgvg_stats* stats, const tgvg_state* init_state = nullptr) {
     if (n < 0 || (n > 0 && (!cubes || !hists || !out)) || (nbins != 8 && nbins != 10) || !params)
         return TGVG_ERR_INVALID;
     if (n == 0) {
@@ -239,19 +249,25 @@ static int minimize_host(tgvg_ctx* ctx, const tgvg_cube* cubes, const uint32_t* 
         return TGVG_OK;
     }
     if (params->init == TGVG_INIT_GIVEN && !u_init) return TGVG_ERR_INVALID;
+    if ((params->init == TGVG_INIT_STATE) != (init_state != nullptr)) return TGVG_ERR_INVALID;
     auto* d_cubes = (tgvg_cube*)ctx->buf(B_T_CUBES, sizeof(tgvg_cube) * n);
     auto* d_hists = (uint32_t*)ctx->buf(B_T_HISTS, sizeof(uint32_t) * nbins * n);
     auto* d_out = (tgvg_state*)ctx->buf(B_T_OUT, sizeof(tgvg_state) * n);
     float* d_u = nullptr;
     if (params->init == TGVG_INIT_GIVEN) d_u = (float*)ctx->buf(B_T_UINIT, sizeof(float) * n);
-    if (!d_cubes || !d_hists || !d_out || (params->init == TGVG_INIT_GIVEN && !d_u)) return TGVG_ERR_NOMEM;
+    tgvg_state* d_s = nullptr;
+    if (init_state) d_s = (tgvg_state*)ctx->buf(B_T_SINIT, sizeof(tgvg_state) * n);
+    if (!d_cubes || !d_hists || !d_out || (params->init == TGVG_INIT_GIVEN && !d_u) || (init_state && !d_s))
+        return TGVG_ERR_NOMEM;
+    if (d_s)
+        TGVG_CK(ctx, cudaMemcpyAsync(d_s, init_state, sizeof(tgvg_state) * n, cudaMemcpyHostToDevice, ctx->stream));
     TGVG_CK(ctx, cudaMemcpyAsync(d_cubes, cubes, sizeof(tgvg_cube) * n, cudaMemcpyHostToDevice, ctx->stream));
     TGVG_CK(ctx, cudaMemcpyAsync(d_hists, hists, sizeof(uint32_t) * nbins * n, cudaMemcpyHostToDevice,
                                  ctx->stream));
     if (d_u)
         TGVG_CK(ctx, cudaMemcpyAsync(d_u, u_init, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream));
     int rc = tgvg::tgv_solve_dev(ctx, d_cubes, d_hists, n, nbins, leaves, nleaf, mode, params, d_u, d_out,
-                                 stats);
+                                 stats, d_s);
     if (rc) return rc;
     TGVG_CK(ctx, cudaMemcpyAsync(out, d_out, sizeof(tgvg_state) * n, cudaMemcpyDeviceToHost, ctx->stream));
     TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -265,6 +281,15 @@ extern "C" int tgvg_tgv_minimize(tgvg_ctx* ctx, const tgvg_cube* cubes, const ui
     if (!ctx) return TGVG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     return minimize_host(ctx, cubes, hists, n, nbins, leaves, nleaf, mode, params, u_init, out, stats);
+}
+
+extern "C" int tgvg_tgv_minimize_state(tgvg_ctx* ctx, const tgvg_cube* cubes, const uint32_t* hists, int64_t n,
+                                       int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, int32_t mode,
+                                       const tgvg_params* params, const tgvg_state* init_state, tgvg_state* out,
+                                       tgvg_stats* stats) {
+    if (!ctx || !params || params->init != TGVG_INIT_STATE || (n > 0 && !init_state)) return TGVG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return minimize_host(ctx, cubes, hists, n, nbins, leaves, nleaf, mode, params, nullptr, out, stats, init_state);
 }
 
 extern "C" int tgvg_tgv_minimize_streaming(tgvg_ctx* ctx, const char* cube_path, const char* hist_path,

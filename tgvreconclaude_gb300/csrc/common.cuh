@@ -146,7 +146,7 @@ enum BufId {
     // Stage 5
     B_H_CUBES, B_H_TEX, B_H_OUT, B_H_CAMS,
     // Stage 6
-    B_T_CUBES, B_T_HISTS, B_T_UINIT, B_T_OUT, B_KEYS, B_DEPTH, B_LEAFOF, B_BUCKET, B_BCOUNT,
+    B_T_CUBES, B_T_HISTS, B_T_UINIT, B_T_SINIT, B_T_OUT, B_KEYS, B_DEPTH, B_LEAFOF, B_BUCKET, B_BCOUNT,
     B_BOFF, B_BTOT, B_PERM, B_INV, B_HKEYS, B_HMIN, B_HMAX, B_NB, B_PAR, B_UV, B_BAR, B_P4, B_Q4,
     B_Q1, B_DAT, B_SNAP, B_LID, B_LEAVES, B_ACC, B_FLAGS, B_RANGES, B_RESID, B_LVSTAT,
     B_BARB, B_P4B, B_Q4B, B_Q1B, B_FSLOT, B_FHALO, B_FHCNT,
@@ -232,7 +232,7 @@ int build_pyramids_dev(tgvg_ctx* ctx, const tgvg_camera* cams, int32_t ncam, flo
 int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists, int64_t n,
                   int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, int32_t mode,
                   const tgvg_params* params, const float* d_u_init, tgvg_state* d_out,
-                  tgvg_stats* stats);
+                  tgvg_stats* stats, const tgvg_state* d_state_init = nullptr);
 int pyramid_dims(int32_t w, int32_t h, int32_t* dims);
 // Exclusive scan of n ints on the context stream; *total receives the sum (synchronises).
 int scan_exclusive(tgvg_ctx* ctx, const int* d_in, int64_t n, int* d_out, int64_t* total);

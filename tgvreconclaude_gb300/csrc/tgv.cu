@@ -249,7 +249,10 @@ __global__ void k_init(int npos, const int* __restrict__ perm, const uint32_t* _
         med = km < NB ? fadd(-1.0f, fdiv(fadd((float)km, 0.5f), NB / 2.0f)) : 1.0f;
         shrink = fmul(0.25f, (float)tot);
     }
-    float u0 = init == TGVG_INIT_MEDIAN ? med : (init == TGVG_INIT_ZERO ? 0.0f : u_init[i]);
+    // TGVG_INIT_STATE: until its level starts a cube holds the reference's
+    // initial state; the caller's state replaces it at the level start.
+    float u0 = (init == TGVG_INIT_MEDIAN || init == TGVG_INIT_STATE) ? med
+             : (init == TGVG_INIT_ZERO ? 0.0f : u_init[i]);
     const float4 s = make_float4(u0, 0.f, 0.f, 0.f);
     uv[p] = s;
     bar[p] = s;
@@ -300,6 +303,25 @@ __global__ void k_parent_init(int o, int n, const int* __restrict__ par, int kee
     P4[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     Q4[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     Q1[p] = 0.f;
+}
+
+// Level start of a whole-state warm start (TGVG_INIT_STATE, no counterpart in
+// the reference): every cube of the level takes the caller's u, v, p and q
+// (TGVCube record of its caller index) in place of the parent copy and the
+// zeroing of p and q; its bars restart from u and v.
+__global__ void k_level_state(int o, int n, const int* __restrict__ perm, const float* __restrict__ st,
+                              float4* __restrict__ uv, float4* __restrict__ bar, float4* __restrict__ P4,
+                              float4* __restrict__ Q4, float* __restrict__ Q1) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int p = o + t;
+    const float* r = st + (size_t)perm[p] * 13;  // 52-byte records: scalar loads
+    const float4 s = make_float4(r[0], r[1], r[2], r[3]);
+    uv[p] = s;
+    bar[p] = s;
+    P4[p] = make_float4(r[4], r[5], r[6], r[7]);
+    Q4[p] = make_float4(r[8], r[9], r[10], r[11]);
+    Q1[p] = r[12];
 }
 
 // Level start: the p/q values that the primal sweep gathers from coarser -x/-y/-z
@@ -2662,14 +2684,17 @@ static int build_wave_tables(tgvg_ctx* ctx, int mode, int min_d, int max_d, cons
 
 int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_hists, int64_t n64,
                   int32_t nbins, const tgvg_leaf* leaves, int32_t nleaf, int32_t mode,
-                  const tgvg_params* prm, const float* d_u_init, tgvg_state* d_out, tgvg_stats* stats) {
+                  const tgvg_params* prm, const float* d_u_init, tgvg_state* d_out, tgvg_stats* stats,
+                  const tgvg_state* d_state_init) {
     tgvg_stats st;
     std::memset(&st, 0, sizeof(st));
     const int64_t k0 = ctx->kernels;
     if (mode < 0 || mode > 2 || (nbins != 8 && nbins != 10) || !prm || n64 < 0 || n64 > POS_MASK)
         return TGVG_ERR_INVALID;
-    if (prm->init < 0 || prm->init > 2 || (prm->init == TGVG_INIT_GIVEN && n64 > 0 && !d_u_init))
+    if (prm->init < 0 || prm->init > TGVG_INIT_STATE || (prm->init == TGVG_INIT_GIVEN && n64 > 0 && !d_u_init) ||
+        (prm->init == TGVG_INIT_STATE && n64 > 0 && !d_state_init))
         return TGVG_ERR_INVALID;
+    const bool level_state = prm->init == TGVG_INIT_STATE;
     if (mode != M_INMEM && nleaf > 0 && !leaves) return TGVG_ERR_INVALID;
     const int n = (int)n64;
     if (n == 0) { if (stats) *stats = st; return TGVG_OK; }
@@ -2940,10 +2965,17 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
             const int Ld = lvl.d, o = lvl.o, cnt = lvl.cnt;
             if (k < TGVG_MAX_LEVELS)
                 TGVG_CK(ctx, record_event(ctx->lev_ev[2 * k], ctx->stream, capturing));
-            if (Ld > min_d) {
-                k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, par, prm->keep_init_u ? 1 : 0,
-                                                                              uv, bar, P4, Q4, Q1);
+            if (level_state) {
+                k_level_state<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(
+                    o, cnt, perm, reinterpret_cast<const float*>(d_state_init), uv, bar, P4, Q4, Q1);
                 TGVG_LAUNCHED(ctx);
+            }
+            if (Ld > min_d) {
+                if (!level_state) {
+                    k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(
+                        o, cnt, par, prm->keep_init_u ? 1 : 0, uv, bar, P4, Q4, Q1);
+                    TGVG_LAUNCHED(ctx);
+                }
                 k_halo<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, n, mode == M_STREAM ? 1 : 0, nb, P4, Q4,
                                                                        Q1, halo);
                 TGVG_LAUNCHED(ctx);
@@ -3010,7 +3042,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         std::vector<uint64_t> key = {
             (uint64_t)mode, (uint64_t)n, (uint64_t)nslot, (uint64_t)iters, (uint64_t)stop,
             (uint64_t)std::max(1, prm->check_every), (uint64_t)(prm->keep_init_u ? 1 : 0), (uint64_t)min_d,
-            (uint64_t)(t_level + 1)};
+            (uint64_t)(t_level + 1), (uint64_t)level_state, (uint64_t)(uintptr_t)d_state_init};
         uint32_t fb[3];
         std::memcpy(&fb[0], &prm->alpha0, 4);
         std::memcpy(&fb[1], &prm->alpha1, 4);
