@@ -173,8 +173,12 @@ def time_cpu_oracle(cubes, hists, iters, nthreads, repeats=1):
 
 
 def run_reference(args):
-    """CPU implementation of the path on the host cores (oracle port of the
-    reference's tgv_minimize; the reference itself is not compiled on this machine)."""
+    """CPU implementation of the path on the host cores: the oracle port of the
+    reference's tgv_minimize (bit-identical to the reference compiled from its
+    own sources, which exist only where the reference is checked out, not on
+    the GPU host), on the same cube slice and iteration count as the FP64
+    check of this package's arm.  All host threads; a single-thread step (the
+    reference's own threading) is reported beside it."""
     import torch
     ws, rank, local, pg = dist_setup()
     if rank != 0:
@@ -186,7 +190,7 @@ def run_reference(args):
     # package runs on this arm.
     w = workloads.build(args.workload, seed=args.seed, device="cuda", histograms=False)
     threads = os.cpu_count() or 1
-    cubes, _ = cpu_sample(w, args.ref_sample, args.cpu_iters)
+    cubes, _ = cpu_sample(w, args.ref_sample or args.cpu_sample, args.cpu_iters)
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import oracle
     oracle.build()
@@ -205,6 +209,7 @@ def run_reference(args):
         tot_li += li
         tot_t += dt
     value = tot_li / tot_t
+    v1, dt1, _ = time_cpu_oracle(cubes, hists, args.cpu_iters, 1)
     sample = f"{len(cubes)} contiguous Morton-ordered cubes of {args.workload}, {args.cpu_iters} iterations per level, in-memory semantics, {threads} threads"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
@@ -212,6 +217,8 @@ def run_reference(args):
             "config": {"workload": args.workload, "cubes_sample": len(cubes), "iters_per_level": args.cpu_iters,
                        "semantics": "tgv_minimize"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "single_thread": {"value": v1, "unit": UNIT, "cores": 1, "seconds": dt1,
+                              "what": "the same step on one thread (the reference is single-threaded)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -308,6 +315,25 @@ def histogram_kernel_eval(ctx, w, cubes_t, nbins, expect, stream, reps=5):
             "frac": nbytes / (ms * 1e-3) / 1e9 / hbm, "peak_kind": peak_kind,
             "texels_on_device_mb": 4 * int(off[-1]) / 1e6,
             "matches_host_call": bool(np.array_equal(d_out.cpu().numpy().view(np.uint32), expect))}
+
+
+def histogram_oracle_check(w, hh, n_sample: int):
+    """Bit-exact check of the GPU histograms against the CPU oracle on a seeded
+    random subset of the workload's cubes, against every depth map."""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as O
+    n = len(w.cubes)
+    rng = np.random.default_rng(12345)
+    idx = np.sort(rng.choice(n, min(n, n_sample), replace=False))
+    maps = [dict(depth=np.ascontiguousarray(d, np.float32), rt_inv=np.array(list(c.rt_inv), np.float32).reshape(4, 4),
+                 fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy, lidar=bool(c.lidar)) for c, d in zip(w.cams, w.depths)]
+    t0 = time.perf_counter()
+    ref = O.compute_histograms(w.cubes[idx], maps, w.cfg["origin"], w.cfg["r_root"], hh.shape[1],
+                               nthreads=os.cpu_count() or 1)
+    dt = time.perf_counter() - t0
+    bad = int((ref != hh[idx]).any(1).sum())
+    return {"cubes": int(len(idx)), "maps": len(maps), "rows_differing": bad, "bit_exact": bad == 0,
+            "votes": int(ref.sum()), "oracle_s": round(dt, 2), "oracle_threads": os.cpu_count() or 1}
 
 
 def surface_eval(args, w, out_t):
@@ -538,7 +564,7 @@ def run_ours(args):
             h_dt = time.perf_counter() - h_t0
             pairs = n * len(w.cams)
             hs = {"pairs_per_s_e2e": pairs / h_dt, "ms_e2e": 1e3 * h_dt, "pairs": pairs,
-                  "matches_workload": bool(np.array_equal(hh, w.hists))}
+                  "oracle_check": histogram_oracle_check(w, hh, args.hist_sample)}
             if w.cams:
                 hs["device"] = histogram_kernel_eval(ctx, w, cubes_t, nbins, hh, stream)
 
@@ -612,7 +638,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-sample", type=int, default=1000000)
     ap.add_argument("--cpu-iters", type=int, default=50)
-    ap.add_argument("--ref-sample", type=int, default=2000000)
+    ap.add_argument("--ref-sample", type=int, default=0, help="reference-arm slice (0: the --cpu-sample slice)")
+    ap.add_argument("--hist-sample", type=int, default=200000, help="cubes checked bit-exact against the oracle")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-hist", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")

@@ -127,6 +127,44 @@ def sphere_rig(n: int, radius: float, target=(0.0, 0.0, 0.0), width=640, height=
     return cams
 
 
+def bounding_radius(prim) -> float:
+    """Radius of a sphere about the primitive's centre that encloses it."""
+    k = prim["kind"]
+    if k == "sphere":
+        return prim["r"]
+    if k == "box":
+        return prim["h"] * math.sqrt(3.0)
+    if k == "torus":
+        return prim["R"] + prim["r"]
+    if k == "cylinder":
+        return math.hypot(prim["r"], prim["h"])
+    raise ValueError(k)
+
+
+def object_rig(scene, n: int, width=2048, height=1536, half_fov_deg: float = 8.0, fill: float = 0.8):
+    """A multi-object capture: camera i looks at primitive i mod P from the
+    next direction of that primitive's Fibonacci sphere, at the distance where
+    the primitive's bounding sphere fills `fill` of the image height.  Narrow
+    fields of view put most pixels on surfaces."""
+    cams = []
+    P = len(scene)
+    ga = math.pi * (3.0 - math.sqrt(5.0))
+    fx = (width / 2.0) / math.tan(math.radians(half_fov_deg))
+    tan_v = (height / 2.0) / fx
+    for i in range(n):
+        j, k = i % P, i // P
+        m = (n - j + P - 1) // P  # cameras of primitive j
+        zc = 1.0 - 2.0 * (k + 0.5) / m
+        rr = math.sqrt(max(0.0, 1.0 - zc * zc))
+        a = ga * k + 2.0 * math.pi * j / P
+        c = np.asarray(scene[j]["c"], np.float64)
+        dist = bounding_radius(scene[j]) / (tan_v * fill)
+        eye = c + np.array([rr * math.cos(a), rr * math.sin(a), zc]) * dist
+        cams.append(dict(rt=look_at(eye, c), fx=fx, fy=fx, cx=width / 2.0, cy=height / 2.0,
+                         width=width, height=height, lidar=False))
+    return cams
+
+
 def terrain_rig(n: int, extent: float, height_above: float, width=1280, height=960,
                 half_fov_deg: float = 30.0, rng: np.random.Generator | None = None):
     """Nadir and oblique cameras over the square [-extent, extent]^2: a grid of

@@ -59,7 +59,9 @@ def make_scene(kind: str, rng):
     raise ValueError(kind)
 
 
-def make_rig(cfg, rng):
+def make_rig(cfg, rng, scene=None):
+    if cfg.get("rig") == "objects":
+        return S.object_rig(scene, cfg["ncam"], cfg["width"], cfg["height"], cfg["half_fov"], cfg.get("fill", 0.8))
     if cfg["scene"] == "terrain":
         return S.terrain_rig(cfg["ncam"], 4.0, cfg["cam_radius"], cfg["width"], cfg["height"], cfg["half_fov"], rng)
     return S.sphere_rig(cfg["ncam"], cfg["cam_radius"], (0.0, 0.0, 0.0), cfg["width"], cfg["height"],
@@ -123,7 +125,7 @@ def build(name: str, seed: int = 0, device: str = "cuda", keep_depths: bool = Fa
     rng = np.random.default_rng(seed)
     t0 = time.time()
     scene = make_scene(cfg["scene"], rng)
-    rig = make_rig(cfg, rng)
+    rig = make_rig(cfg, rng, scene)
     dtype = torch.float32 if device != "cpu" else torch.float64
     Ps, Rs, depths, cams = [], [], [], []
     for i, c in enumerate(rig):
