@@ -248,7 +248,9 @@ int tgvg_compute_histograms_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, int64_t
  * library holds on every GPU that loads it: at most 256 cameras and
  * 16 Mi pyramid texels (64 MiB, levels 0.. of all maps together); larger
  * requests return TGVG_ERR_LIMIT.  The first call on a device looks the array
- * up on that device (make it before any stream capture).  Work is enqueued on
+ * up on that device, which may load this library's device code and the array
+ * with it: make that first call before any stream capture, and before the
+ * caller reserves the device's memory for its own pool.  Work is enqueued on
  * `stream` (a cudaStream_t; null = the legacy default stream) and the call
  * returns without waiting.  All calls share the one array, so calls that may
  * overlap on the GPU (other streams, other host threads) race and must be

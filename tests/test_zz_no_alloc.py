@@ -64,6 +64,36 @@ def test_noalloc_matches_regular_entry_on_two_calls_in_a_row():
         assert np.array_equal(got, want)
 
 
+def test_noalloc_call_leaves_free_device_memory_unchanged():
+    """After a first call on the device (which may load the library's device
+    code together with its scratch array), a call allocates nothing: the
+    device's free memory is the same before and after it."""
+    import torch
+    cams, depths, cubes, nbins = _scene(3, 4, 256, 192, 8, 20000)
+    dev_maps = [torch.from_numpy(d).cuda() for d in depths]
+    d_cubes = torch.from_numpy(cubes.view(np.int32).reshape(len(cubes), 4)).cuda()
+    d_out = torch.zeros((len(cubes), nbins), dtype=torch.int32, device="cuda")
+    arr = (N.Camera * len(cams))(*cams)
+    bases = (C.c_void_p * len(cams))(*[t.data_ptr() for t in dev_maps])
+    origin = np.array([-1.5, -1.5, -1.5], np.float32)
+    stream = torch.cuda.current_stream()
+
+    def call():
+        rc = N.lib().tgvg_compute_histograms_noalloc(d_cubes.data_ptr(), len(cubes), arr, len(cams), bases,
+                                                     origin.ctypes.data, C.c_float(1.5), nbins, d_out.data_ptr(),
+                                                     stream.cuda_stream)
+        assert rc == 0, N.lib().tgvg_strerror(rc)
+        stream.synchronize()
+
+    call()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        call()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert int(d_out.sum()) > 0
+
+
 def test_noalloc_rejects_requests_beyond_its_scratch():
     lib = N.lib()
     big = N.Camera()
