@@ -120,6 +120,54 @@ static inline void finish_thresholds(Thresholds& thr) {
         if (!(thr.t[k] > std::ldexp(1.0f, k - 1) && thr.t[k] <= std::ldexp(1.0f, k))) thr.expo = 0;
 }
 
+// Camera cull for one block of cubes (no counterpart in the reference; it
+// only skips pairs that project() rejects, histogram.cpp:76-106).  The
+// block's cube centres lie in the box ctr +- ext.  A pair is accepted only if
+// its camera-space z > 0 and the truncated pixel coordinates fall inside the
+// image, i.e. -1 < x fx / z + cx < W and -1 < y fy / z + cy < H; for z > 0 these
+// are half-spaces g(P) > 0 with g linear in the world point P.  The float
+// evaluation of project() differs from exact arithmetic by a few units of
+// 2^-24 of the magnitudes involved, so if the largest g over the box is below
+// minus 1e-3 of those magnitudes, no centre in the box can pass: the camera is
+// skipped for the whole block.  Cameras with a non-finite parameter are never
+// skipped.
+__device__ __noinline__ bool camera_may_see(const DevCam& c, const float* ctr, const float* ext) {
+    const float* m = c.m;
+    bool finite = isfinite(c.fx) && isfinite(c.fy) && isfinite(c.cx) && isfinite(c.cy);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) finite = finite && isfinite(m[k]);
+    if (!finite) return true;
+    // S_r: the magnitude of row r's terms over the box (rows x, y, z of Rt_inv)
+    float S[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        float t = fabsf(m[4 * r + 3]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) t += fabsf(m[4 * r + k]) * (fabsf(ctr[k]) + ext[k]);
+        S[r] = t;
+    }
+    // largest value over the box of g = wr * (row r) + wz * (row z); the error of
+    // this float evaluation is a few 1e-7 of the magnitudes, far inside the margin
+    auto max_g = [&](int r, float wr, float wz) {
+        float g = wr * m[4 * r + 3] + wz * m[11];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float a = wr * m[4 * r + k] + wz * m[8 + k];
+            g += a * ctr[k] + fabsf(a) * ext[k];
+        }
+        return g;
+    };
+    if (max_g(0, 0.0f, 1.0f) < -1e-3f * S[2]) return false;  // z > 0
+    const float W = (float)c.W, H = (float)c.H;
+    const float tu = 1e-3f * (fabsf(c.fx) * S[0] + (fabsf(c.cx) + W + 2.0f) * S[2]);
+    const float tv = 1e-3f * (fabsf(c.fy) * S[1] + (fabsf(c.cy) + H + 2.0f) * S[2]);
+    if (max_g(0, c.fx, c.cx + 1.0f) < -tu) return false;  // x fx / z + cx > -1
+    if (max_g(0, -c.fx, W - c.cx) < -tu) return false;    // x fx / z + cx < W
+    if (max_g(1, c.fy, c.cy + 1.0f) < -tv) return false;  // y fy / z + cy > -1
+    if (max_g(1, -c.fy, H - c.cy) < -tv) return false;    // y fy / z + cy < H
+    return true;
+}
+
 // PACK: the bin counts are kept as 16-bit fields of 64-bit words (four bins a
 // word), which holds when no cube can collect more than 65535 votes; one shift
 // and a few predicated adds per pair instead of a compare and add per bin.
@@ -130,6 +178,9 @@ k_histograms(const uint4* __restrict__ cubes, int64_t n, const DevCam* __restric
              Thresholds thr, uint32_t* __restrict__ out) {
     __shared__ DevCam s_cam[CAM_BATCH];
     __shared__ float s_thr[13];
+    __shared__ bool s_vis[CAM_BATCH];
+    __shared__ float s_box[HIST_BLOCK / 32][6];
+    __shared__ float s_geo[6];  // centre and half extent of the block's box; ext < 0: no active cube
     if (threadIdx.x < 13) s_thr[threadIdx.x] = thr.t[threadIdx.x];
     const int64_t i = int64_t(blockIdx.x) * HIST_BLOCK + threadIdx.x;
     const bool valid = i < n;
@@ -162,6 +213,36 @@ k_histograms(const uint4* __restrict__ cubes, int64_t n, const DevCam* __restric
     const float eta = fmul(18.0f, r_c);
     const float HALF = NB / 2.0f;
 
+    // bounding box of the block's active cube centres (empty: every camera skipped,
+    // which changes nothing since no thread of the block is active)
+    {
+        float b[6] = {active ? px : INFINITY, active ? py : INFINITY, active ? pz : INFINITY,
+                      active ? px : -INFINITY, active ? py : -INFINITY, active ? pz : -INFINITY};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                b[k] = fminf(b[k], __shfl_xor_sync(0xffffffffu, b[k], o));
+                b[k + 3] = fmaxf(b[k + 3], __shfl_xor_sync(0xffffffffu, b[k + 3], o));
+            }
+        }
+        if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s_box[threadIdx.x >> 5][k] = b[k];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        float lo = INFINITY, hi = -INFINITY;
+        for (int w = 0; w < HIST_BLOCK / 32; ++w) { lo = fminf(lo, s_box[w][k]); hi = fmaxf(hi, s_box[w][k + 3]); }
+        const bool any = lo <= hi;
+        // the centre's rounding is covered by rounding the half extent up
+        const float ctr = 0.5f * (lo + hi);
+        s_geo[k] = any ? ctr : 0.0f;
+        s_geo[k + 3] = any ? fmaxf(hi - ctr, ctr - lo) * 1.0001f : -1.0f;
+    }
+
     for (int c0 = 0; c0 < ncam; c0 += CAM_BATCH) {
         const int nb = min(CAM_BATCH, ncam - c0);
         __syncthreads();
@@ -172,8 +253,12 @@ k_histograms(const uint4* __restrict__ cubes, int64_t n, const DevCam* __restric
             for (int w = threadIdx.x; w < words; w += HIST_BLOCK) dst[w] = src[w];
         }
         __syncthreads();
+        if (threadIdx.x < nb)
+            s_vis[threadIdx.x] = s_geo[3] >= 0.0f && camera_may_see(s_cam[threadIdx.x], s_geo, s_geo + 3);
+        __syncthreads();
         if (!active) continue;
         for (int cc = 0; cc < nb; ++cc) {
+            if (!s_vis[cc]) continue;  // block-uniform: no centre of the block can pass project()
             const DevCam& c = s_cam[cc];
             // project (histogram.cpp:76-106): cam = Rt_inv * [P, 1]
             float X = fmul(c.m[0], px); X = fadd(X, fmul(c.m[1], py)); X = fadd(X, fmul(c.m[2], pz));
