@@ -433,31 +433,78 @@ def stages13_eval(args, w):
 def warm_start_eval(args):
     """Time to relative residual 1e-4 (at most 6000 iterations per level) on
     held-out small scenes: zero start, trained network, reference initialisation."""
-    from tgvreconclaude_gb300 import api, warmstart as WS
-    path = os.path.join(HERE, "tgvreconclaude_gb300", "data", "warmstart_nb10.npz")
-    if not os.path.exists(path):
+    from tgvreconclaude_gb300 import warmstart as WS
+    if not os.path.exists(WS.WEIGHTS):
         return {"unavailable": "no trained weights at tgvreconclaude_gb300/data/warmstart_nb10.npz"}
-    mlp = WS.WarmStartMLP.load(path)
-    recs = []
-    for seed in range(1000, 1000 + args.warm_seeds):
-        kind = "torus" if seed % 2 == 0 else "three"
-        cubes, hists = WS.small_scene(seed, kind)
-        zero, warm, _ = WS.compare(mlp, cubes, hists, tol=1e-4)
-        prm = api.TGVParams(alpha0=WS.SOLVE["alpha0"], alpha1=WS.SOLVE["alpha1"], iters=6000, tol=1e-4,
-                            check_every=10)
-        _, st = api.tgv_solve(cubes, hists, None, "inmem", prm)
-        recs.append(dict(seed=seed, kind=kind, cubes=int(len(cubes)), zero_ms=zero.device_ms,
-                         warm_ms=warm.device_ms + warm.predict_ms, ref_ms=st["total_ms"],
-                         zero_leaf_iters=zero.leaf_iters, warm_leaf_iters=warm.leaf_iters,
-                         ref_leaf_iters=st["leaf_iters"],
-                         capped_levels=[sum(i >= 6000 for i in r) for r in (zero.iters, warm.iters, st["iters_run"])]))
-    med = lambda k: float(np.median([r[k] for r in recs]))
+    mlp = WS.WarmStartMLP.load(WS.WEIGHTS)
+    recs, summary = WS.evaluate(mlp, range(1000, 1000 + args.warm_seeds), tol=1e-4)
     return {"tol": 1e-4, "max_iters_per_level": 6000, "scenes": len(recs), "graphs": "off (direct launches)",
             "scene": "16 cameras at 320x240, torus (depth 7) / three objects (depth 8), held-out seeds 1000+",
-            "median_zero_ms": med("zero_ms"), "median_warm_ms": med("warm_ms"), "median_ref_ms": med("ref_ms"),
-            "time_ratio_zero_over_warm": float(np.median([r["zero_ms"] / r["warm_ms"] for r in recs])),
-            "leaf_iters_ratio_zero_over_warm": med("zero_leaf_iters") / med("warm_leaf_iters"),
-            "records": recs}
+            **summary, "records": recs}
+
+
+def time_to_gap_eval(args):
+    """The batched-chunks configuration with 12 primitives (prims256: 256 cameras
+    at 2048x1536, 128 chunks, streaming semantics) solved to relative residual
+    1e-4 (at most 6000 iterations per level) on the device from the zero start,
+    from the learned warm start and from the reference's initialisation; device
+    time per solve (CUDA events on the library stream), prediction included."""
+    import torch
+    from tgvreconclaude_gb300 import api, warmstart as WS, workloads
+    t0 = time.time()
+    w = workloads.build(args.ttg_workload, seed=args.seed, device="cuda")
+    gen_s = time.time() - t0
+    torch.cuda.empty_cache()
+    ctx = api.context()
+    n = len(w.cubes)
+    cubes_t = torch.from_numpy(w.cubes.view(np.int32).reshape(n, 4)).cuda()
+    hists_t = torch.from_numpy(w.hists.view(np.int32)).cuda()
+    out_t = torch.empty((n, 13), dtype=torch.float32, device="cuda")
+    prm = api.TGVParams(alpha0=2.0, alpha1=1.0, iters=6000, tol=1e-4, check_every=10)
+    res = {"workload": args.ttg_workload, "cubes": n, "chunks": int(len(w.leaves)), "cameras": len(w.cams),
+           "image": f"{w.cfg['width']}x{w.cfg['height']}",
+           "levels": {int(k): int(v) for k, v in enumerate(np.bincount(w.cubes["depth"], minlength=22)) if v},
+           "gen_s": round(gen_s, 1), "tol": 1e-4, "max_iters_per_level": 6000, "graphs": "off (direct launches)"}
+    ctx.set_graphs(False)
+    try:
+        starts = {"zero": torch.zeros((n, 13), dtype=torch.float32, device="cuda")}
+        pred_ms = 0.0
+        if os.path.exists(WS.WEIGHTS):
+            mlp = WS.WarmStartMLP.load(WS.WEIGHTS)
+            u_t = torch.empty(n, dtype=torch.float32, device="cuda")
+            st = torch.cuda.ExternalStream(ctx.stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            lv = np.ascontiguousarray(w.leaves)
+            e0.record(st)
+            ctx.check(ctx.lib.tgvg_mlp_warm_start_dev(ctx.h, mlp.h, cubes_t.data_ptr(), hists_t.data_ptr(), n,
+                                                      w.hists.shape[1], lv.ctypes.data, len(lv), u_t.data_ptr()),
+                      "tgvg_mlp_warm_start_dev")
+            with torch.cuda.stream(st):
+                rec = torch.zeros((n, 13), dtype=torch.float32, device="cuda")
+                rec[:, 0] = u_t
+            e1.record(st)
+            torch.cuda.synchronize()
+            pred_ms = e0.elapsed_time(e1)
+            starts["warm"] = rec
+        for name in ("zero", "warm", "reference"):
+            if name == "reference":
+                st = api.tgv_solve_device(cubes_t, hists_t, out_t, w.leaves, "stream", prm)
+            elif name in starts:
+                st = api.tgv_solve_device(cubes_t, hists_t, out_t, w.leaves, "stream", prm,
+                                          state_init_t=starts[name])
+            else:
+                continue
+            ms = st["total_ms"] + (pred_ms if name == "warm" else 0.0)
+            res[name] = {"ms": round(ms, 2), "leaf_iters": int(st["leaf_iters"]), "iters": st["iters_run"],
+                         "active": [int(a) for a in st["active"]],
+                         "capped_levels": int(sum(i >= prm.iters for i in st["iters_run"]))}
+        if "warm" in res:
+            res["warm"]["predict_ms"] = round(pred_ms, 3)
+            res["time_ratio_zero_over_warm"] = res["zero"]["ms"] / res["warm"]["ms"]
+            res["time_ratio_reference_over_warm"] = res["reference"]["ms"] / res["warm"]["ms"]
+    finally:
+        ctx.set_graphs(True)
+    return res
 
 
 def run_ours(args):
@@ -591,6 +638,7 @@ def run_ours(args):
         surf = {} if args.skip_surface else surface_eval(args, w, out_t)
         s13 = {} if args.skip_stages13 else stages13_eval(args, w)
         ws_eval = {} if args.skip_warm else warm_start_eval(args)
+        ttg = {} if args.skip_ttg else time_to_gap_eval(args)
 
         depth_hist = np.bincount(w.cubes["depth"], minlength=22)
         result = {
@@ -609,6 +657,7 @@ def run_ours(args):
             "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "fp64_check": f64, "histograms": hs, "surface": surf,
             "stages_1_3": s13,
             "warm_start": ws_eval,
+            "time_to_gap": ttg,
             "clocks": clk, "graph": last_st["graph"],
             "gpu_launches": int(launches), "leaf_iters_per_step": int(li_all / args.steps),
             "levels_detail": [{"depth": d, "active": int(a), "ms": round(m, 3), "schedule": s, "iters": it,
@@ -649,7 +698,9 @@ def main():
     ap.add_argument("--tol", type=float, default=0.0,
                     help="solve each level to this relative residual (time to tolerance) instead of a fixed count")
     ap.add_argument("--max-iters", type=int, default=6000, help="iteration cap per level with --tol")
-    ap.add_argument("--warm-seeds", type=int, default=6)
+    ap.add_argument("--warm-seeds", type=int, default=20)
+    ap.add_argument("--skip-ttg", action="store_true", help="skip the time-to-gap solves of --ttg-workload")
+    ap.add_argument("--ttg-workload", default="prims256")
     ap.add_argument("--max-cubes", type=int, default=0, help="truncate the workload (profiling runs)")
     ap.add_argument("--cache", default="", help="load the workload from / save it to this .npz (profiling runs)")
     ap.add_argument("--schedules", default="", help="fix schedules, e.g. 17:15,21:14 (size class:schedule; profiling runs)")

@@ -97,8 +97,9 @@ def test_trained_network_gain():
         err = WS.start_errors(m, cubes[ok], hists[ok], ref[ok])
         assert err["network"] < 0.25 * err["zero"], err
         assert err["network"] <= 1.05 * err["median"], err
-        zero, warm, out = WS.compare(m, cubes, hists, tol=1e-4)
-        print(seed, err, "leaf-iterations zero %d warm %d" % (zero.leaf_iters, warm.leaf_iters))
+        r, out = WS.compare(m, cubes, hists, tol=1e-4)
+        print(seed, err, "leaf-iterations zero %d warm %d reference %d" % (
+            r["zero"].leaf_iters, r["warm"].leaf_iters, r["reference"].leaf_iters))
         # the end points agree wherever both solves stay bounded (the unstable
         # cubes can drift in one solve and not the other)
         both = ok & (np.abs(out["u"]) <= 1.0)

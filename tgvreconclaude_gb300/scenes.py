@@ -165,6 +165,28 @@ def object_rig(scene, n: int, width=2048, height=1536, half_fov_deg: float = 8.0
     return cams
 
 
+def primitives_in_view(scene, cam, margin_deg: float = 2.0):
+    """The primitives whose bounding sphere reaches into the camera's view cone
+    (the cone around the optical axis through the image corners).  Sphere
+    tracing only these finds the same surfaces at a fraction of the cost when
+    each camera frames one object with a narrow field of view."""
+    rt = np.asarray(cam["rt"], np.float64)
+    eye, axis = rt[:3, 3], rt[:3, 2]
+    half_diag = math.atan(math.hypot(cam["width"] / 2.0 / cam["fx"], cam["height"] / 2.0 / cam["fy"]))
+    out = []
+    for p in scene:
+        d = np.asarray(p["c"], np.float64) - eye
+        dist = float(np.linalg.norm(d))
+        rb = bounding_radius(p)
+        if dist <= rb:
+            out.append(p)
+            continue
+        ang = math.acos(max(-1.0, min(1.0, float(np.dot(d, axis)) / dist)))
+        if ang - math.asin(rb / dist) <= half_diag + math.radians(margin_deg):
+            out.append(p)
+    return out
+
+
 def terrain_rig(n: int, extent: float, height_above: float, width=1280, height=960,
                 half_fov_deg: float = 30.0, rng: np.random.Generator | None = None):
     """Nadir and oblique cameras over the square [-extent, extent]^2: a grid of
@@ -236,6 +258,8 @@ def render_depth(scene, cam, seed: int, device="cpu", steps: int = 160, max_dist
     dtype = dtype or torch.float64
     eps = 1e-6 if dtype == torch.float64 else 2e-5
     W, H = cam["width"], cam["height"]
+    if not scene:
+        return torch.full((H, W), float("nan"), dtype=torch.float32, device=device)
     rt = torch.tensor(np.asarray(cam["rt"], np.float64), device=device, dtype=dtype)
     gen = torch.Generator(device=device).manual_seed(int(seed))
     out = torch.empty((H, W), dtype=torch.float32, device=device)
@@ -285,13 +309,16 @@ def three_objects_scene(rng: np.random.Generator):
                  sigma=float(s[2]))]
 
 
-def primitives_scene(rng: np.random.Generator, n: int = 12, sigma: float = 0.004):
+def primitives_scene(rng: np.random.Generator, n: int = 12, sigma: float = 0.004, size=(0.25, 0.6),
+                     spread: float = 1.8):
+    """`n` seeded spheres, boxes, tori and cylinders (in turn) of size drawn from
+    `size`, centred in [-spread, spread]^3."""
     kinds = ["sphere", "box", "torus", "cylinder"]
     out = []
     for i in range(n):
         k = kinds[i % 4]
-        c = tuple(rng.uniform(-1.8, 1.8, 3))
-        s = float(rng.uniform(0.25, 0.6))
+        c = tuple(rng.uniform(-spread, spread, 3))
+        s = float(rng.uniform(*size))
         if k == "sphere":
             out.append(dict(kind=k, c=c, r=s, sigma=sigma))
         elif k == "box":

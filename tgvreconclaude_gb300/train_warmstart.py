@@ -9,9 +9,10 @@
    per level); cubes whose converged |u| > 1.5 (no fixed point) are left out.
 2. Training: this package's forward/backward/Adam kernels on the GPU.
 3. Evaluation on `--eval` held-out seeds: iterations and time to a relative
-   residual of 1e-4 for the solver from a zero start (every level from u = 0),
-   from the network's prediction, and (for reference) from the reference
-   initialisation (median, then the parent's u at each level).
+   residual of 1e-4 for the solver from a zero start (every level from
+   u = v = p = q = 0), from the network's prediction (every level from the
+   predicted u), and from the reference initialisation (median, then the
+   parent's u and v at each level); all three solve the reference's problem.
 Prints one JSON line with the per-seed records and the medians.
 """
 from __future__ import annotations
@@ -54,28 +55,7 @@ def main(argv=None):
         info = {"train_scenes": a.train, "samples": int(len(X)), "data_s": round(t1 - t0, 1),
                 "train_s": round(t2 - t1, 1), "loss_initial": loss0, "loss_final": loss, "weights": a.out}
 
-    recs = []
-    for seed in range(1000, 1000 + a.eval):
-        kind = "torus" if seed % 2 == 0 else "three"
-        cubes, hists = WS.small_scene(seed, kind)
-        zero, warm, out = WS.compare(mlp, cubes, hists, tol=a.tol)
-        prm = api.TGVParams(alpha0=WS.SOLVE["alpha0"], alpha1=WS.SOLVE["alpha1"], iters=6000, tol=a.tol,
-                            check_every=10)
-        _, st = api.tgv_solve(cubes, hists, None, "inmem", prm)
-        recs.append(dict(seed=seed, kind=kind, cubes=int(len(cubes)),
-                         zero_leaf_iters=zero.leaf_iters, zero_ms=zero.device_ms, zero_levels=zero.iters,
-                         warm_leaf_iters=warm.leaf_iters, warm_ms=warm.device_ms, warm_levels=warm.iters,
-                         warm_predict_ms=warm.predict_ms, ref_leaf_iters=st["leaf_iters"], ref_ms=st["total_ms"],
-                         ref_levels=st["iters_run"]))
-    med = lambda k: float(np.median([r[k] for r in recs]))
-    summary = {
-        "iters_ratio_zero_over_warm": med("zero_leaf_iters") / med("warm_leaf_iters"),
-        "time_ratio_zero_over_warm": float(np.median([r["zero_ms"] / (r["warm_ms"] + r["warm_predict_ms"])
-                                                       for r in recs])),
-        "iters_ratio_ref_over_warm": med("ref_leaf_iters") / med("warm_leaf_iters"),
-        "median_zero_ms": med("zero_ms"), "median_warm_ms": med("warm_ms"), "median_ref_ms": med("ref_ms"),
-        "median_predict_ms": med("warm_predict_ms"),
-    }
+    recs, summary = WS.evaluate(mlp, range(1000, 1000 + a.eval), tol=a.tol)
     print(json.dumps({"info": info, "summary": summary, "records": recs}), flush=True)
 
 

@@ -7,9 +7,10 @@ median indicator, the reference's own start; the warm start is median +
 network.  It is trained on the GPU by this package's own forward/backward
 kernels (include/tgvg.h, tgvg_mlp_*) on pairs that the plain solver produces
 on seeded scenes, and it seeds a solve with params.init = "given" and
-keep_init_u = True: every level starts from the prediction instead of the
-parent's u.  The plain primal-dual iterations still run to the same stopping
-tolerance, so the prediction only changes how many iterations that takes.
+every level starts from the prediction (tgvg_tgv_minimize_state records with
+v = p = q = 0) instead of the parent copy.  The plain primal-dual iterations
+still run to the same stopping tolerance, so the prediction only changes how
+many iterations that takes.
 """
 from __future__ import annotations
 
@@ -188,14 +189,32 @@ class SolveRecord:
     predict_ms: float = 0.0
 
 
-def time_to_tol(cubes, hists, u0=None, tol: float = 1e-4, max_iters: int = 6000, check_every: int = 10):
-    """Solve to relative residual `tol` from a zero start (u0 None) or from u0,
-    every level keeping its initial u.  Returns a SolveRecord."""
-    init = "zero" if u0 is None else "given"
+def start_records(n: int, u=None) -> np.ndarray:
+    """Whole-state records (tgvg_tgv_minimize_state) that start every level from
+    u (zero when None) with v = p = q = 0."""
+    s = np.zeros(n, F.STATE_DTYPE)
+    if u is not None:
+        s["u"] = u
+    return s
+
+
+def time_to_tol(cubes, hists, start: str = "zero", u0=None, tol: float = 1e-4, max_iters: int = 6000,
+                check_every: int = 10, leaves=None, mode: str = "inmem"):
+    """Solve to relative residual `tol` and return (state, SolveRecord).
+
+    All starts solve the reference's problem: cubes hold the reference's
+    initial state until their level starts.  start = "reference": the
+    reference's initialisation (median, then the parent's u and v at each
+    level); "zero": every level from u = v = p = q = 0; "warm": every level
+    from u = u0 with v = p = q = 0."""
     prm = api.TGVParams(alpha0=SOLVE["alpha0"], alpha1=SOLVE["alpha1"], iters=max_iters, tol=tol,
-                        check_every=check_every, init=init, keep_init_u=True)
+                        check_every=check_every)
     t0 = time.perf_counter()
-    out, st = api.tgv_solve(cubes, hists, None, "inmem", prm, u_init=u0)
+    if start == "reference":
+        out, st = api.tgv_solve(cubes, hists, leaves, mode, prm)
+    else:
+        out, st = api.tgv_solve(cubes, hists, leaves, mode, prm,
+                                state_init=start_records(len(cubes), u0 if start == "warm" else None))
     wall = 1e3 * (time.perf_counter() - t0)
     return out, SolveRecord(st["leaf_iters"], st["iters_run"], st["total_ms"], wall)
 
@@ -219,21 +238,54 @@ def start_errors(mlp: WarmStartMLP, cubes, hists, u_conv) -> dict:
     return dict(zero=rms(np.zeros_like(u_conv)), median=rms(median_start(hists)), network=rms(pred))
 
 
-def compare(mlp: WarmStartMLP, cubes, hists, tol: float = 1e-4):
-    """Zero start vs warm start on one problem (both to the same tolerance).
+def compare(mlp: WarmStartMLP, cubes, hists, tol: float = 1e-4, leaves=None, mode: str = "inmem"):
+    """The zero start, the learned warm start and the reference's initialisation
+    on one problem, each to the same tolerance -> dict of SolveRecords and the
+    warm solve's state.
 
-    Both solves run with direct launches: the warm solve is the second sighting
-    of the same problem, and with level-loop graphs on it would pay for the
-    graph's capture and instantiation while the zero solve did not."""
+    The solves run with direct launches: later sightings of the same problem
+    would otherwise pay for, or profit from, the level-loop graph's capture."""
     ctx = api.context()
     ctx.set_graphs(False)
     try:
-        _, zero = time_to_tol(cubes, hists, None, tol)
+        _, zero = time_to_tol(cubes, hists, "zero", tol=tol, leaves=leaves, mode=mode)
         t0 = time.perf_counter()
-        u0 = mlp.warm_start(cubes, hists)
+        u0 = mlp.warm_start(cubes, hists, leaves)
         pred_ms = 1e3 * (time.perf_counter() - t0)
-        out, warm = time_to_tol(cubes, hists, u0, tol)
+        out, warm = time_to_tol(cubes, hists, "warm", u0, tol, leaves=leaves, mode=mode)
+        _, ref = time_to_tol(cubes, hists, "reference", tol=tol, leaves=leaves, mode=mode)
     finally:
         ctx.set_graphs(True)
     warm.predict_ms = pred_ms
-    return zero, warm, out
+    return dict(zero=zero, warm=warm, reference=ref), out
+
+
+def evaluate(mlp: WarmStartMLP, seeds, tol: float = 1e-4, max_iters: int = 6000):
+    """Held-out evaluation on small scenes (torus on even seeds, three objects
+    on odd ones): time and leaf-iterations to relative residual `tol` from the
+    zero start, from the network's prediction and from the reference's
+    initialisation.  Returns (records, summary)."""
+    recs = []
+    for seed in seeds:
+        kind = "torus" if seed % 2 == 0 else "three"
+        cubes, hists = small_scene(seed, kind)
+        r, _ = compare(mlp, cubes, hists, tol=tol)
+        rec = dict(seed=seed, kind=kind, cubes=int(len(cubes)), predict_ms=r["warm"].predict_ms)
+        for k, v in r.items():
+            rec[f"{k}_ms"] = v.device_ms + (v.predict_ms if k == "warm" else 0.0)
+            rec[f"{k}_leaf_iters"] = v.leaf_iters
+            rec[f"{k}_iters"] = v.iters
+            rec[f"{k}_capped_levels"] = sum(i >= max_iters for i in v.iters)
+        recs.append(rec)
+    med = lambda k: float(np.median([r[k] for r in recs]))
+    ratio = lambda a, b: float(np.median([r[f"{a}_ms"] / r[f"{b}_ms"] for r in recs]))
+    summary = {
+        "time_ratio_zero_over_warm": ratio("zero", "warm"),
+        "time_ratio_reference_over_warm": ratio("reference", "warm"),
+        "leaf_iters_ratio_zero_over_warm": med("zero_leaf_iters") / med("warm_leaf_iters"),
+        "leaf_iters_ratio_reference_over_warm": med("reference_leaf_iters") / med("warm_leaf_iters"),
+        "median_zero_ms": med("zero_ms"), "median_warm_ms": med("warm_ms"), "median_reference_ms": med("reference_ms"),
+        "median_predict_ms": med("predict_ms"),
+        "scenes_with_capped_levels": int(sum(r["zero_capped_levels"] > 0 for r in recs)),
+    }
+    return recs, summary

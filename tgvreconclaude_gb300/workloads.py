@@ -11,7 +11,9 @@ computed by this package's own Stage-5 kernels -> chunk leaves.
               64 cameras at 1920x1080; max depth 11; 10 bins; 1000 iterations
   terrain128  8 seeded sinusoids (amplitude 0.1-0.5) + N(0,0.003) over [-4,4]^2; 128 nadir/oblique
               cameras at 1280x960; max depth 12; 64 chunks of log-uniform 50k-4M cubes
-  prims256    12 seeded primitives, sigma 0.004; 256 cameras at 2048x1536; max depth 13; 128 chunks
+  prims256    12 seeded primitives (sphere, box, torus, cylinder in turn; size 0.45-0.9), sigma 0.004;
+              256 cameras at 2048x1536, each framing one primitive with a 16-degree field of view
+              (21-22 views per primitive); max depth 13; 128 chunks
 """
 from __future__ import annotations
 
@@ -30,7 +32,8 @@ CONFIGS = {
                     origin=(-3.0, -3.0, -3.0), r_root=3.0, max_depth=11, nbins=10, iters=1000, chunks=1),
     "terrain128": dict(scene="terrain", ncam=128, cam_radius=4.0, width=1280, height=960, half_fov=30.0,
                        origin=(-4.0, -4.0, -4.0), r_root=4.0, max_depth=12, nbins=10, iters=1000, chunks=64),
-    "prims256": dict(scene="prims", ncam=256, cam_radius=7.0, width=2048, height=1536, half_fov=25.0,
+    "prims256": dict(scene="prims", rig="objects", prim_size=(0.45, 0.9), ncam=256, cam_radius=7.0, width=2048,
+                     height=1536, half_fov=8.0,
                      origin=(-3.0, -3.0, -3.0), r_root=3.0, max_depth=13, nbins=10, iters=1000, chunks=128),
 }
 
@@ -47,7 +50,7 @@ class Workload:
     timings: dict = field(default_factory=dict)
 
 
-def make_scene(kind: str, rng):
+def make_scene(kind: str, rng, size=None):
     if kind == "torus":
         return S.torus_scene(0.005)
     if kind == "three":
@@ -55,7 +58,7 @@ def make_scene(kind: str, rng):
     if kind == "terrain":
         return S.terrain_scene(rng)
     if kind == "prims":
-        return S.primitives_scene(rng, 12, 0.004)
+        return S.primitives_scene(rng, 12, 0.004, size=size or (0.25, 0.6))
     raise ValueError(kind)
 
 
@@ -124,12 +127,13 @@ def build(name: str, seed: int = 0, device: str = "cuda", keep_depths: bool = Fa
     cfg = dict(CONFIGS[name])
     rng = np.random.default_rng(seed)
     t0 = time.time()
-    scene = make_scene(cfg["scene"], rng)
+    scene = make_scene(cfg["scene"], rng, cfg.get("prim_size"))
     rig = make_rig(cfg, rng, scene)
     dtype = torch.float32 if device != "cpu" else torch.float64
     Ps, Rs, depths, cams = [], [], [], []
     for i, c in enumerate(rig):
-        d = S.render_depth(scene, c, seed=seed * 100003 + i, device=device, dtype=dtype)
+        seen = S.primitives_in_view(scene, c) if cfg.get("rig") == "objects" else scene
+        d = S.render_depth(seen, c, seed=seed * 100003 + i, device=device, dtype=dtype)
         P, r = S.samples_from_depth_map(d, c, torch)
         Ps.append(P)
         Rs.append(r)
