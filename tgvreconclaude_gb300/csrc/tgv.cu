@@ -2512,7 +2512,23 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
     std::vector<int> cands;
     if ((rc = tune_candidates<MODE>(ctx, n, stop, cands))) return rc;
     if (!stop && (int)cands.size() * TUNE_SEG * 2 <= iters) { *cfg = -1; return TGVG_OK; }
-    *cfg = n <= 65536 ? 3 : CFG_BAND;  // untuned default: one cooperative launch for small units, else band order
+    // Untuned default (a tolerance-stopped solve, or too few iterations to
+    // tune), after the autotuner's picks on the benchmark octrees: the unit's
+    // state held on chip by one block (small units) or one cluster of 16 CTAs
+    // (mid-size units), else band order.  Each is a single launch for all of
+    // the unit's iterations or one launch per sweep, with no grid-wide barrier.
+    *cfg = CFG_BAND;
+    if (n <= SMEM_MAX_N) {
+        if ((rc = smem_level_setup<MODE>(ctx))) return rc;
+        *cfg = effective_cfg<MODE>(ctx, CFG_SMEM, n);
+    } else if (n <= CTA_MAX_N) {
+        *cfg = CFG_CTA;
+    } else if (n <= CLUSTER_MAX_N) {
+        int cs = 0;
+        if ((rc = cluster_capacity<MODE>(ctx, stop, &cs))) return rc;
+        if (cs >= 16) *cfg = CFG_CLUSTER16;
+        else if (cs >= 8) *cfg = CFG_CLUSTER8;
+    }
     return TGVG_OK;
 }
 
