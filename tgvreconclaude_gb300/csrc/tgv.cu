@@ -3003,11 +3003,14 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                 k_copy4<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, bar, snap);
                 TGVG_LAUNCHED(ctx);
             }
+            // Every slot's iteration count starts at the full count: the fused
+            // schedules' settle step reads it in fixed-count solves too, so a
+            // count left by an earlier tolerance-stopped solve must not survive.
+            k_fill_i32<<<blocks_for(nslot, 128), 128, 0, ctx->stream>>>(nslot, iters_run, iters);
+            TGVG_LAUNCHED(ctx);
             if (stop) {
                 TGVG_CK(ctx, cudaMemsetAsync(acc, 0, 32ull * nslot, ctx->stream));
                 TGVG_CK(ctx, cudaMemsetAsync(done, 0, 4ull * nslot, ctx->stream));
-                k_fill_i32<<<blocks_for(nslot, 128), 128, 0, ctx->stream>>>(nslot, iters_run, iters);
-                TGVG_LAUNCHED(ctx);
                 TGVG_CK(ctx, cudaMemsetAsync(resid, 0, 8ull * nslot, ctx->stream));
             }
             // NVTX range per level so profilers can select the largest level's launches
