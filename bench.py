@@ -465,6 +465,11 @@ def time_to_gap_eval(args):
            "image": f"{w.cfg['width']}x{w.cfg['height']}",
            "levels": {int(k): int(v) for k, v in enumerate(np.bincount(w.cubes["depth"], minlength=22)) if v},
            "gen_s": round(gen_s, 1), "tol": 1e-4, "max_iters_per_level": 6000, "graphs": "off (direct launches)"}
+    # Stage 5 on the same workload: the binning kernel alone, and a bit-exact
+    # check of its histograms against the oracle on a sample of cubes
+    hs = histogram_kernel_eval(ctx, w, cubes_t, w.hists.shape[1], w.hists, torch.cuda.ExternalStream(ctx.stream))
+    hs["oracle_check"] = histogram_oracle_check(w, w.hists, args.hist_sample // 4)
+    res["histograms"] = hs
     ctx.set_graphs(False)
     try:
         starts = {"zero": torch.zeros((n, 13), dtype=torch.float32, device="cuda")}
