@@ -11,7 +11,7 @@ computed by this package's own Stage-5 kernels -> chunk leaves.
               64 cameras at 1920x1080; max depth 11; 10 bins; 1000 iterations
   terrain128  8 seeded sinusoids (amplitude 0.1-0.5) + N(0,0.003) over [-4,4]^2; 128 nadir/oblique
               cameras at 1280x960; max depth 12; 64 chunks of log-uniform 50k-4M cubes
-  prims256    12 seeded primitives (sphere, box, torus, cylinder in turn; size 0.5-1.0), sigma 0.004;
+  prims256    12 seeded primitives (sphere, box, torus, cylinder in turn; size 0.55-1.1, centres in [-1.7, 1.7]^3), sigma 0.004;
               256 cameras at 2048x1536, each framing one primitive with a 16-degree field of view
               (21-22 views per primitive); max depth 13; 128 chunks
 """
@@ -32,7 +32,7 @@ CONFIGS = {
                     origin=(-3.0, -3.0, -3.0), r_root=3.0, max_depth=11, nbins=10, iters=1000, chunks=1),
     "terrain128": dict(scene="terrain", ncam=128, cam_radius=4.0, width=1280, height=960, half_fov=30.0,
                        origin=(-4.0, -4.0, -4.0), r_root=4.0, max_depth=12, nbins=10, iters=1000, chunks=64),
-    "prims256": dict(scene="prims", rig="objects", prim_size=(0.5, 1.0), ncam=256, cam_radius=7.0, width=2048,
+    "prims256": dict(scene="prims", rig="objects", prim_size=(0.55, 1.1), prim_spread=1.7, ncam=256, cam_radius=7.0, width=2048,
                      height=1536, half_fov=8.0,
                      origin=(-3.0, -3.0, -3.0), r_root=3.0, max_depth=13, nbins=10, iters=1000, chunks=128),
 }
@@ -50,7 +50,7 @@ class Workload:
     timings: dict = field(default_factory=dict)
 
 
-def make_scene(kind: str, rng, size=None):
+def make_scene(kind: str, rng, size=None, spread=None):
     if kind == "torus":
         return S.torus_scene(0.005)
     if kind == "three":
@@ -58,7 +58,7 @@ def make_scene(kind: str, rng, size=None):
     if kind == "terrain":
         return S.terrain_scene(rng)
     if kind == "prims":
-        return S.primitives_scene(rng, 12, 0.004, size=size or (0.25, 0.6))
+        return S.primitives_scene(rng, 12, 0.004, size=size or (0.25, 0.6), spread=spread or 1.8)
     raise ValueError(kind)
 
 
@@ -127,7 +127,7 @@ def build(name: str, seed: int = 0, device: str = "cuda", keep_depths: bool = Fa
     cfg = dict(CONFIGS[name])
     rng = np.random.default_rng(seed)
     t0 = time.time()
-    scene = make_scene(cfg["scene"], rng, cfg.get("prim_size"))
+    scene = make_scene(cfg["scene"], rng, cfg.get("prim_size"), cfg.get("prim_spread"))
     rig = make_rig(cfg, rng, scene)
     dtype = torch.float32 if device != "cpu" else torch.float64
     Ps, Rs, depths, cams = [], [], [], []
