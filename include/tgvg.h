@@ -128,7 +128,10 @@ typedef struct tgvg_stats {
     int32_t kt_fused;                    /* 1: the timed level ran the fused kernel, 2: the
                                             wavefront kernel (kt_dual_ms holds its time,
                                             kt_primal_ms 0)                                   */
-    int32_t reserved;
+    int32_t placement;                   /* 0: state in device memory; 1: the solve exceeded
+                                            the device budget (tgvg_set_device_budget) and its
+                                            state lived in host memory, each level's slice
+                                            prefetched to the device while it ran            */
     /* No counterpart in the reference: the FP64 primal energy of level slot k's
      * state when the level ends, sum over its cubes of tot |u - median| +
      * alpha1 |grad u - v| + alpha0 |e(v)| with the iteration's own difference
@@ -199,6 +202,17 @@ int tgvg_set_schedule(tgvg_ctx* ctx, int32_t mode, int32_t cls, int32_t cfg);
  * (graph = 1), so one-shot solves run with direct launches (graph = 0).
  * Results do not depend on it. */
 int tgvg_set_graphs(tgvg_ctx* ctx, int on);
+/* Device budget for one solve, in bytes (0 = none, the default).  A solve whose
+ * device footprint (about 400 B per cube) would exceed it keeps its per-cube
+ * state -- u, v, p, q, bars, the streaming snapshot and the fused schedules'
+ * second set -- in host memory (CUDA managed memory preferring the host), and
+ * moves each level's slice to the device while that level runs and back after
+ * it; keys, hash and neighbour tables stay in device memory.  On a GB300 the
+ * host memory is the Grace CPU's, reached over NVLink-C2C.  Such solves run
+ * with direct launches (no level-loop graph).  This is the out-of-core
+ * streaming of tgv_minimize_streaming (reference tgv.cpp:802-1070) for
+ * problems beyond device memory; results do not depend on it. */
+int tgvg_set_device_budget(tgvg_ctx* ctx, int64_t bytes);
 
 /* ---- Stage 5: depth maps -> histograms ------------------------------------ */
 

@@ -103,7 +103,7 @@ class Stats(C.Structure):
                 ("kt_depth", C.c_int32), ("kt_launches", C.c_int32), ("kt_active", C.c_int64),
                 ("kt_dual_ms", C.c_double), ("kt_primal_ms", C.c_double),
                 ("level_ms", C.c_double * MAX_LEVELS), ("schedule", C.c_int32 * MAX_LEVELS),
-                ("kt_fused", C.c_int32), ("reserved", C.c_int32), ("energy", C.c_double * MAX_LEVELS)]
+                ("kt_fused", C.c_int32), ("placement", C.c_int32), ("energy", C.c_double * MAX_LEVELS)]
 
     def as_dict(self):
         k = self.n_levels
@@ -115,6 +115,7 @@ class Stats(C.Structure):
                     kt_depth=self.kt_depth, kt_launches=self.kt_launches, kt_active=self.kt_active,
                     kt_dual_ms=self.kt_dual_ms, kt_primal_ms=self.kt_primal_ms,
                     level_ms=list(self.level_ms[:k]), schedule=list(self.schedule[:k]), kt_fused=self.kt_fused,
+                    placement=self.placement,
                     energy=list(self.energy[:k]))
 
 
@@ -131,6 +132,7 @@ _SIGS = {
     "tgvg_set_timing": ([P, C.c_int], C.c_int),
     "tgvg_set_schedule": ([P, C.c_int32, C.c_int32, C.c_int32], C.c_int),
     "tgvg_set_graphs": ([P, C.c_int], C.c_int),
+    "tgvg_set_device_budget": ([P, C.c_int64], C.c_int),
     "tgvg_pyramid_dims": ([C.c_int32, C.c_int32, P], C.c_int),
     "tgvg_build_pyramids": ([P, P, C.c_int32, P, P], C.c_int),
     "tgvg_compute_histograms": ([P, P, C.c_int64, P, C.c_int32, P, P, C.c_float, C.c_int32, P], C.c_int),

@@ -15,6 +15,14 @@
 void* tgvg_ctx::buf(int id, size_t bytes) {
     if (bytes == 0) bytes = 16;
     Buf& b = bufs[id];
+    if (b.cap >= bytes && !b.managed) return b.p;
+    if (b.p && b.managed) {
+        cudaStreamSynchronize(stream);
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+        b.managed = false;
+    }
     if (b.cap >= bytes) return b.p;
     if (b.p) {
         cudaStreamSynchronize(stream);
@@ -36,6 +44,39 @@ void* tgvg_ctx::buf(int id, size_t bytes) {
         return nullptr;
     }
     b.cap = want;
+    return b.p;
+}
+
+void* tgvg_ctx::host_backed(int id, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    Buf& b = bufs[id];
+    if (b.cap >= bytes && b.managed) return b.p;
+    if (b.p) {
+        cudaStreamSynchronize(stream);
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    b.managed = false;
+    cudaError_t e = cudaMallocManaged(&b.p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b.p = nullptr;
+        last_error = "cudaMallocManaged of " + std::to_string(bytes) + " bytes failed";
+        return nullptr;
+    }
+    cudaMemLocation host{};
+    host.type = cudaMemLocationTypeHost;
+    cudaMemLocation dev{};
+    dev.type = cudaMemLocationTypeDevice;
+    dev.id = device;
+    // pages stay in host memory unless prefetched; the device maps what it
+    // touches otherwise instead of faulting it over page by page
+    if (cudaMemAdvise(b.p, bytes, cudaMemAdviseSetPreferredLocation, host) != cudaSuccess ||
+        cudaMemAdvise(b.p, bytes, cudaMemAdviseSetAccessedBy, dev) != cudaSuccess)
+        cudaGetLastError();  // advice only: placement stays correct without it
+    b.cap = bytes;
+    b.managed = true;
     return b.p;
 }
 
@@ -89,6 +130,13 @@ extern "C" int tgvg_set_graphs(tgvg_ctx* ctx, int on) {
     if (!ctx) return TGVG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->graphs = on != 0;
+    return TGVG_OK;
+}
+
+extern "C" int tgvg_set_device_budget(tgvg_ctx* ctx, int64_t bytes) {
+    if (!ctx || bytes < 0) return TGVG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->device_budget = (size_t)bytes;
     return TGVG_OK;
 }
 
@@ -250,9 +298,13 @@ static int minimize_host(tgvg_ctx* ctx, const tgvg_cube* cubes, const uint32_t* 
     }
     if (params->init == TGVG_INIT_GIVEN && !u_init) return TGVG_ERR_INVALID;
     if ((params->init == TGVG_INIT_STATE) != (init_state != nullptr)) return TGVG_ERR_INVALID;
-    auto* d_cubes = (tgvg_cube*)ctx->buf(B_T_CUBES, sizeof(tgvg_cube) * n);
-    auto* d_hists = (uint32_t*)ctx->buf(B_T_HISTS, sizeof(uint32_t) * nbins * n);
-    auto* d_out = (tgvg_state*)ctx->buf(B_T_OUT, sizeof(tgvg_state) * n);
+    // beyond the device budget the staged inputs and the output live in host memory too
+    auto TB = [&](int id, size_t bytes) {
+        return state_paged(ctx, n) ? ctx->host_backed(id, bytes) : ctx->buf(id, bytes);
+    };
+    auto* d_cubes = (tgvg_cube*)TB(B_T_CUBES, sizeof(tgvg_cube) * n);
+    auto* d_hists = (uint32_t*)TB(B_T_HISTS, sizeof(uint32_t) * nbins * n);
+    auto* d_out = (tgvg_state*)TB(B_T_OUT, sizeof(tgvg_state) * n);
     float* d_u = nullptr;
     if (params->init == TGVG_INIT_GIVEN) d_u = (float*)ctx->buf(B_T_UINIT, sizeof(float) * n);
     tgvg_state* d_s = nullptr;

@@ -173,7 +173,7 @@ struct tgvg_ctx {
     std::mutex mu;
     std::string last_error;
     int64_t kernels = 0;
-    struct Buf { void* p = nullptr; size_t cap = 0; };
+    struct Buf { void* p = nullptr; size_t cap = 0; bool managed = false; };
     Buf bufs[B_COUNT];
     float lvl_thresh[13] = {};  // footprint thresholds of pyramid levels 1..12
     cudaEvent_t ev[4] = {};
@@ -197,6 +197,8 @@ struct tgvg_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     int64_t graph_kernels = 0;         // kernel nodes in the cached graph
     bool capturing = false;            // the level loop is being captured
+    size_t device_budget = 0;          // solve footprint above which the state lives in host memory (0: never)
+    bool paged_now = false;            // the running solve's state lives in host memory (no TMA-staged schedule)
     tgvg_ctx() {
         for (auto& m : tune)
             for (int& c : m) c = -1;
@@ -205,9 +207,20 @@ struct tgvg_ctx {
     // Device buffer `id` with room for `bytes` (grow-only; contents are not kept
     // across growth).  Returns nullptr after recording the error.
     void* buf(int id, size_t bytes);
+    // The same as managed memory whose pages live in host memory until they
+    // are prefetched to the device (the state of solves larger than the
+    // device budget).  A buffer changes kind by being reallocated.
+    void* host_backed(int id, size_t bytes);
     int fail(int rc, const std::string& what);
     int cuda_fail(cudaError_t e, const char* what);
 };
+
+// Device bytes of a solve of n cubes, in round figures: state and its second
+// set 136 B, keys, hash, neighbour and order tables about 150 B, inputs and
+// output of a host-buffer call about 110 B per cube.
+static inline bool state_paged(const tgvg_ctx* ctx, int64_t n) {
+    return ctx->device_budget > 0 && uint64_t(n) * 400ull > ctx->device_budget;
+}
 
 #define TGVG_CK(ctx, call)                                                   \
     do {                                                                     \

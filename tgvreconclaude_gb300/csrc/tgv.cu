@@ -2450,7 +2450,7 @@ static int tune_candidates(tgvg_ctx* ctx, int n, bool stop, std::vector<int>& ca
     }
     if (MODE != M_OC && ctx->fuse_cur) {
         cands.push_back(CFG_FUSED);
-        cands.push_back(CFG_FUSED_TMA);
+        if (!ctx->paged_now) cands.push_back(CFG_FUSED_TMA);  // bulk copies stay on device-resident state
     }
     return TGVG_OK;
 }
@@ -2467,7 +2467,8 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
     int rc = iter_occupancy<MODE>(ctx), cmax = 0;
     if (!rc) rc = coop_capacity<MODE>(ctx, stop, &cmax);
     if (rc) return rc;
-    const int tuned = ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, n))];
+    int tuned = ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, n))];
+    if (tuned == CFG_FUSED_TMA && ctx->paged_now) tuned = CFG_FUSED;  // bulk copies stay on device-resident state
     if (timed) {  // per-launch event timing needs one of the per-sweep-launch or fused schedules
         *cfg = (per_launch_cfg(tuned) || ((fused_cfg(tuned) || wave_cfg(tuned)) && MODE != M_OC)) ? tuned : CFG_BAND;
         if (fused_cfg(*cfg)) {
@@ -2760,13 +2761,19 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     auto* hmax = (int*)B(B_HMAX, 4ull * cap);
     auto* nb = (int*)B(B_NB, 4ull * 6 * n + 64);  // padded: staged slices round up to 16 B
     auto* par = (int*)B(B_PAR, 4ull * n);
-    auto* uv = (float4*)B(B_UV, 16ull * n);
-    auto* bar = (float4*)B(B_BAR, 16ull * n);
-    auto* P4 = (float4*)B(B_P4, 16ull * n);
-    auto* Q4 = (float4*)B(B_Q4, 16ull * n);
-    auto* Q1 = (float*)B(B_Q1, 4ull * n + 64);
+    // Beyond the device budget the per-cube state (and its snapshot and second
+    // set) lives in host memory and each level's slice is prefetched to the
+    // device while the level runs; keys, hash and neighbour tables stay resident.
+    const bool paged = state_paged(ctx, n64);
+    ctx->paged_now = paged;
+    auto SB = [&](int id, size_t bytes) { return paged ? ctx->host_backed(id, bytes) : ctx->buf(id, bytes); };
+    auto* uv = (float4*)SB(B_UV, 16ull * n);
+    auto* bar = (float4*)SB(B_BAR, 16ull * n);
+    auto* P4 = (float4*)SB(B_P4, 16ull * n);
+    auto* Q4 = (float4*)SB(B_Q4, 16ull * n);
+    auto* Q1 = (float*)SB(B_Q1, 4ull * n + 64);
     auto* dat = (float2*)B(B_DAT, 8ull * n + 64);
-    auto* snap = (float4*)B(B_SNAP, mode == M_INMEM ? 16 : 16ull * n);
+    auto* snap = (float4*)SB(B_SNAP, mode == M_INMEM ? 16 : 16ull * n);
     auto* lid = (int*)B(B_LID, 4ull * n);
     auto* lv = (int*)B(B_LEAVES, 4ull * (3 * std::max(1, nsl) + 2 * std::max(1, L)));
     auto* acc = (double*)B(B_ACC, 32ull * nslot);
@@ -2865,10 +2872,10 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     if (mode != M_OC && fiters > 0 && n_act > 0) {
         int64_t total_tiles = 0;
         for (int Ld = min_d; Ld <= max_d; ++Ld) total_tiles += (h_bstart[Ld + 1] - h_bstart[Ld] + FT - 1) / FT;
-        auto* barB = (float4*)B(B_BARB, 16ull * n);
-        auto* P4B = (float4*)B(B_P4B, 16ull * n);
-        auto* Q4B = (float4*)B(B_Q4B, 16ull * n);
-        auto* Q1B = (float*)B(B_Q1B, 4ull * n + 64);
+        auto* barB = (float4*)SB(B_BARB, 16ull * n);
+        auto* P4B = (float4*)SB(B_P4B, 16ull * n);
+        auto* Q4B = (float4*)SB(B_Q4B, 16ull * n);
+        auto* Q1B = (float*)SB(B_Q1B, 4ull * n + 64);
         auto* fslot = (int*)B(B_FSLOT, 12ull * n + 64);
         auto* fhalo = (int*)B(B_FHALO, 4ull * FH * std::max<int64_t>(1, total_tiles));
         auto* fhcnt = (int*)B(B_FHCNT, 4ull * std::max<int64_t>(1, total_tiles));
@@ -2974,11 +2981,26 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     // iteration counts / residuals stay on the device (copied per level into
     // lv_it / lv_res) and are read once after the loop, so the sequence can be
     // captured into a CUDA graph.
+    // Host-backed state: move a level's slice of every state array to the
+    // device before the level runs, and back to host memory after it.
+    auto page = [&](int o, int cnt, bool in) -> int {
+        cudaMemLocation loc{};
+        loc.type = in ? cudaMemLocationTypeDevice : cudaMemLocationTypeHost;
+        loc.id = in ? ctx->device : 0;
+        float4* a16[] = {uv, bar, P4, Q4};
+        for (float4* a : a16) TGVG_CK(ctx, cudaMemPrefetchAsync(a + o, 16ull * cnt, loc, 0, ctx->stream));
+        TGVG_CK(ctx, cudaMemPrefetchAsync(Q1 + o, 4ull * cnt, loc, 0, ctx->stream));
+        return TGVG_OK;
+    };
     auto enqueue = [&](bool capturing) -> int {
         TGVG_CK(ctx, cudaMemsetAsync(lv_en, 0, 8ull * TGVG_MAX_LEVELS, ctx->stream));
         for (int k = 0; k < (int)levels.size(); ++k) {
             const Level& lvl = levels[k];
             const int Ld = lvl.d, o = lvl.o, cnt = lvl.cnt;
+            if (paged) {
+                const int rc = page(o, cnt, true);
+                if (rc) return rc;
+            }
             if (k < TGVG_MAX_LEVELS)
                 TGVG_CK(ctx, record_event(ctx->lev_ev[2 * k], ctx->stream, capturing));
             if (level_state) {
@@ -3052,11 +3074,16 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                                                                                     prm->alpha0, prm->alpha1, lv_en + k);
                 TGVG_LAUNCHED(ctx);
             }
+            if (paged) {
+                const int rc = page(o, cnt, false);
+                if (rc) return rc;
+            }
         }
         return TGVG_OK;
     };
 
-    if (ctx->graphs && !tuning && !levels.empty()) {
+    // (host-backed state runs with direct launches: its prefetches are not captured)
+    if (ctx->graphs && !tuning && !levels.empty() && !paged) {
         // Problem signature: everything the captured launches bake in.
         std::vector<uint64_t> key = {
             (uint64_t)mode, (uint64_t)n, (uint64_t)nslot, (uint64_t)iters, (uint64_t)stop,
@@ -3209,6 +3236,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         st.kt_dual_ms = dsum;
         st.kt_primal_ms = psum;
     }
+    st.placement = paged ? 1 : 0;
     if (stats) *stats = st;
     return TGVG_OK;
 }
