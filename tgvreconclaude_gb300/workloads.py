@@ -107,15 +107,33 @@ def chunk_leaves(cubes, k: int, rng, lo=50_000, hi=4_000_000):
     return leaves
 
 
+_CAM_FIELDS = ("fx", "fy", "cx", "cy", "width", "height", "lidar")
+
+
 def save(w: Workload, path: str) -> None:
-    """Cubes, histograms and leaves of a workload (no depth maps) as one .npz."""
-    np.savez(path, name=w.name, cubes=w.cubes, hists=w.hists, leaves=w.leaves)
+    """Cubes, histograms, leaves, cameras and depth maps of a workload as one .npz
+    (so that a profiled run can skip the ray casting)."""
+    extra = {}
+    if w.cams and w.depths is not None and len({d.shape for d in w.depths}) == 1:
+        extra["depths"] = np.stack([np.asarray(d, np.float32) for d in w.depths])
+        extra["cam_rt_inv"] = np.array([list(c.rt_inv) for c in w.cams], np.float32)
+        extra["cam_par"] = np.array([[getattr(c, f) for f in _CAM_FIELDS] for c in w.cams], np.float64)
+    np.savez(path, name=w.name, cubes=w.cubes, hists=w.hists, leaves=w.leaves, **extra)
 
 
 def load(path: str) -> Workload:
     d = np.load(path)
     name = str(d["name"])
-    return Workload(name, dict(CONFIGS[name]), [], None, d["cubes"], d["hists"], d["leaves"], {})
+    cams, depths = [], None
+    if "depths" in d.files:
+        depths = list(d["depths"])
+        for rt, par in zip(d["cam_rt_inv"], d["cam_par"]):
+            c = N.Camera()
+            c.rt_inv[:] = [float(v) for v in rt]
+            c.fx, c.fy, c.cx, c.cy = (float(v) for v in par[:4])
+            c.width, c.height, c.lidar = (int(v) for v in par[4:])
+            cams.append(c)
+    return Workload(name, dict(CONFIGS[name]), cams, depths, d["cubes"], d["hists"], d["leaves"], {})
 
 
 def build(name: str, seed: int = 0, device: str = "cuda", keep_depths: bool = False,
