@@ -352,6 +352,30 @@ def test_tgv_stopping_rule(oracle_lib):
         assert_state_equal(out, ref, f"stop {mode}")
 
 
+@pytest.mark.parametrize("mode", ["inmem", "stream"])
+def test_tgv_autotuned_stopping_solves(oracle_lib, mode):
+    """Tolerance-stopped solves with a large iteration cap tune their untuned
+    size classes online; levels that meet the tolerance during the trials end
+    there.  States and per-level iteration counts equal the oracle's; a second
+    solve reuses the tuned table."""
+    ctx = api.context()
+    rng = np.random.default_rng(88)
+    cubes = S.random_octree(rng, dmin=1, dmax=7, target=60000, shape="sphere")
+    hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.0)
+    leaves = S.split_leaves(len(cubes), 5, rng, cubes, aligned=True)
+    ref, rst = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 3000, tol=2e-4, check_every=10,
+                                    nthreads=8)
+    ctx.set_schedule(mode, -1, -1)
+    try:
+        for _ in range(2):
+            out, st = api.tgv_solve(cubes, hists, leaves, mode,
+                                    api.TGVParams(2.0, 1.0, 3000, tol=2e-4, check_every=10))
+            assert_state_equal(out, ref, f"tuned stopping {mode}")
+            assert st["iters_run"] == [r["iters_run"] for r in rst]
+    finally:
+        ctx.set_schedule(mode, -1, -1)
+
+
 def test_tgv_reference_kats():
     """tests/test_stage6.cpp:25-184 through the GPU API."""
     cubes = F.make_cubes([int(F.morton_encode(np.uint32(ix << 16), np.uint32(0), np.uint32(0))) for ix in range(3)],

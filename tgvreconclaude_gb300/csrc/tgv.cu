@@ -2512,7 +2512,10 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
     }
     std::vector<int> cands;
     if ((rc = tune_candidates<MODE>(ctx, n, stop, cands))) return rc;
-    if (!stop && (int)cands.size() * TUNE_SEG * 2 <= iters) { *cfg = -1; return TGVG_OK; }
+    // Tune when the trials are at most half the iterations: fixed-count solves,
+    // and tolerance-stopped solves with a large cap (a unit that meets its
+    // tolerance during the trials ends there without recording a pick).
+    if ((int)cands.size() * TUNE_SEG * 2 <= iters) { *cfg = -1; return TGVG_OK; }
     // Untuned default (a tolerance-stopped solve, or too few iterations to
     // tune), after the autotuner's picks on the benchmark octrees: the unit's
     // state held on chip by one block (small units) or one cluster of 16 CTAs
@@ -2524,7 +2527,7 @@ static int plan_schedule(tgvg_ctx* ctx, int n, int iters, bool stop, bool timed,
         *cfg = effective_cfg<MODE>(ctx, CFG_SMEM, n);
     } else if (n <= CTA_MAX_N) {
         *cfg = CFG_CTA;
-    } else if (n <= CLUSTER_MAX_N) {
+    } else if (n <= 8192) {  // one cluster covers 16 SMs: beyond this per-sweep launches are faster
         int cs = 0;
         if ((rc = cluster_capacity<MODE>(ctx, stop, &cs))) return rc;
         if (cs >= 16) *cfg = CFG_CLUSTER16;
@@ -2542,15 +2545,25 @@ static int run_unit_t(tgvg_ctx* ctx, IterArgs& a, int iters, bool stop, bool tim
         if ((rc = tune_candidates<MODE>(ctx, a.n, stop, cands))) return rc;
         float best_ms = 1e30f;
         int best = 0;
+        const int ns = unit_slots<MODE>(a.nslot);
+        std::vector<int> done_h(stop ? ns : 0);
         for (int c : cands) {
             TGVG_CK(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
             if ((rc = run_segment<MODE>(ctx, a, c, it, TUNE_SEG, stop, false))) return rc;
             TGVG_CK(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
             TGVG_CK(ctx, cudaEventSynchronize(ctx->ev[3]));
+            it += TUNE_SEG;
+            if (stop) {
+                // A unit that met its tolerance during the trials is finished: its
+                // last segment stopped early, so nothing is recorded for the class.
+                TGVG_CK(ctx, cudaMemcpy(done_h.data(), a.done + a.slot0, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+                bool all = true;
+                for (int d : done_h) all = all && d != 0;
+                if (all) { *used = effective_cfg<MODE>(ctx, c, a.n); return TGVG_OK; }
+            }
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
             if (ms < best_ms) { best_ms = ms; best = c; }
-            it += TUNE_SEG;
         }
         ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, a.n))] = best;
         cfg = best;
