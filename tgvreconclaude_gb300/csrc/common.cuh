@@ -162,7 +162,7 @@ enum BufId {
     B_P_OUT, B_P_TMP,
     // ordered-wavefront schedule tables
     B_W_KEYS, B_W_SKEYS, B_W_KEEP, B_W_POS, B_W_UKEYS, B_W_DEP, B_W_DOFF, B_W_FLAG, B_W_CNT, B_W_TMP, B_W_TMP2,
-    B_W_GSTART, B_LVENERGY, B_HALO,
+    B_W_GSTART, B_LVENERGY,
     B_COUNT
 };
 

@@ -324,31 +324,6 @@ __global__ void k_level_state(int o, int n, const int* __restrict__ perm, const 
     Q1[p] = r[12];
 }
 
-// Level start: the p/q values that the primal sweep gathers from coarser -x/-y/-z
-// neighbours (positions before the level), in the order primal_load_gather uses
-// them, one float4 per cube and face: halo[k * n + t] for face 2k+1 of cube o + t.
-// Entries of other faces are never read.  The BORDER flag marks a border cube
-// (read as zero) in streaming semantics, but only an out-of-leaf cube (p/q read
-// live, so gathered here too) in OC semantics.
-__global__ void k_halo(int o, int n, int npos, int stream, const int* __restrict__ nb, const float4* __restrict__ P4,
-                       const float4* __restrict__ Q4, const float* __restrict__ Q1, float4* __restrict__ halo) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int p = o + t;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const int jr = nb[(size_t)(2 * k + 1) * npos + p];
-        if (jr < 0 || (stream && (jr & BORDER)) || (jr & POS_MASK) >= o) continue;
-        const int j = jr & POS_MASK;
-        const float4 a4 = P4[j], b4 = Q4[j];
-        float4 h;
-        if (k == 0) h = make_float4(a4.x, a4.w, b4.z, b4.w);
-        else if (k == 1) h = make_float4(a4.y, b4.x, b4.z, Q1[j]);
-        else h = make_float4(a4.z, b4.y, b4.w, Q1[j]);
-        halo[(size_t)k * n + t] = h;
-    }
-}
-
 // Streaming level start: every cube's bars restart from its state u/v, and the
 // frozen copy for border reads is taken (build_bars_frozen, tgv.cpp:606-635).
 __global__ void k_stream_snapshot(int npos, const float4* __restrict__ uv, float4* __restrict__ bar,
@@ -392,8 +367,6 @@ struct IterArgs {
     int swap;             // per-launch schedules: dual sweep in reverse order, primal forward
     int band;             // per-launch schedules: warps stride over the whole unit (grid-stride band)
     int lend;             // end of the level's positions; cubes at lend and beyond are deeper
-    int lbeg;             // first position of the level; cubes before it are coarser
-    const float4* halo;   // [3][lend - lbeg]: coarser -x/-y/-z neighbours' gathered p/q (null: gather)
 };
 
 // Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
@@ -553,46 +526,26 @@ __device__ __forceinline__ void primal_load_own(const IterArgs& a, int p, Primal
 // a deeper cube (an octant-0 descendant shares the code, tgv.cpp:97-109,369-370).
 // Levels run coarse to fine, so a deeper cube's p/q still hold their initial
 // zeros while this level runs: such a neighbour reads as 0 without a load.
-// A coarser neighbour's p/q do not change while this level runs either: with a
-// halo, its four gathered values come from the cube's own record of that face
-// (built by k_halo at the level start), a coalesced load instead of three
-// scattered ones into the previous levels' arrays.
 template <int MODE, bool CG>
 __device__ __forceinline__ void primal_load_gather(const IterArgs& a, int p, PrimalLd& L) {
     const int j1 = L.j1, j3 = L.j3, j5 = L.j5;
     L.gp10 = L.gq10 = L.gq13 = L.gq14 = 0.f;
     L.gp31 = L.gq31 = L.gq33 = L.gq35 = 0.f;
     L.gp52 = L.gq52 = L.gq54 = L.gq55 = 0.f;
-    const int hn = a.lend - a.lbeg, hp = p - a.lbeg;
     if (j1 >= 0 && !(MODE == M_STREAM && (j1 & BORDER)) && (j1 & POS_MASK) < a.lend) {
         const int j = j1 & POS_MASK;
-        if (a.halo && j < a.lbeg) {
-            const float4 h = ld4<CG>(a.halo + hp);
-            L.gp10 = h.x; L.gq10 = h.y; L.gq13 = h.z; L.gq14 = h.w;
-        } else {
-            const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
-            L.gp10 = a4.x; L.gq10 = a4.w; L.gq13 = b4.z; L.gq14 = b4.w;
-        }
+        const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
+        L.gp10 = a4.x; L.gq10 = a4.w; L.gq13 = b4.z; L.gq14 = b4.w;
     }
     if (j3 >= 0 && !(MODE == M_STREAM && (j3 & BORDER)) && (j3 & POS_MASK) < a.lend) {
         const int j = j3 & POS_MASK;
-        if (a.halo && j < a.lbeg) {
-            const float4 h = ld4<CG>(a.halo + hn + hp);
-            L.gp31 = h.x; L.gq31 = h.y; L.gq33 = h.z; L.gq35 = h.w;
-        } else {
-            const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
-            L.gp31 = a4.y; L.gq31 = b4.x; L.gq33 = b4.z; L.gq35 = ld1<CG>(a.Q1 + j);
-        }
+        const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
+        L.gp31 = a4.y; L.gq31 = b4.x; L.gq33 = b4.z; L.gq35 = ld1<CG>(a.Q1 + j);
     }
     if (j5 >= 0 && !(MODE == M_STREAM && (j5 & BORDER)) && (j5 & POS_MASK) < a.lend) {
         const int j = j5 & POS_MASK;
-        if (a.halo && j < a.lbeg) {
-            const float4 h = ld4<CG>(a.halo + 2 * hn + hp);
-            L.gp52 = h.x; L.gq52 = h.y; L.gq54 = h.z; L.gq55 = h.w;
-        } else {
-            const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
-            L.gp52 = a4.z; L.gq52 = b4.y; L.gq54 = b4.w; L.gq55 = ld1<CG>(a.Q1 + j);
-        }
+        const float4 a4 = ld4<CG>(a.P4 + j), b4 = ld4<CG>(a.Q4 + j);
+        L.gp52 = a4.z; L.gq52 = b4.y; L.gq54 = b4.w; L.gq55 = ld1<CG>(a.Q1 + j);
     }
 }
 
@@ -2985,10 +2938,6 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     std::vector<int> used(nlv, -1);
     auto* lv_en = (double*)B(B_LVENERGY, 8ull * TGVG_MAX_LEVELS);
     if (!lv_en) return TGVG_ERR_NOMEM;
-    int max_cnt = 0;
-    for (const Level& lvl : levels) max_cnt = std::max(max_cnt, lvl.cnt);
-    auto* halo = (float4*)B(B_HALO, 48ull * std::max(max_cnt, 1));
-    if (!halo) return TGVG_ERR_NOMEM;
 
     // Enqueue every level.  Device-only work: stopping flags and per-level
     // iteration counts / residuals stay on the device (copied per level into
@@ -3021,14 +2970,9 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                     o, cnt, perm, reinterpret_cast<const float*>(d_state_init), uv, bar, P4, Q4, Q1);
                 TGVG_LAUNCHED(ctx);
             }
-            if (Ld > min_d) {
-                if (!level_state) {
-                    k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(
-                        o, cnt, par, prm->keep_init_u ? 1 : 0, uv, bar, P4, Q4, Q1);
-                    TGVG_LAUNCHED(ctx);
-                }
-                k_halo<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(o, cnt, n, mode == M_STREAM ? 1 : 0, nb, P4, Q4,
-                                                                       Q1, halo);
+            if (Ld > min_d && !level_state) {
+                k_parent_init<<<blocks_for(cnt, 256), 256, 0, ctx->stream>>>(
+                    o, cnt, par, prm->keep_init_u ? 1 : 0, uv, bar, P4, Q4, Q1);
                 TGVG_LAUNCHED(ctx);
             }
             if (mode == M_STREAM) {
@@ -3054,8 +2998,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
             for (const Unit& u : lvl.us) {
                 IterArgs a;
                 std::memset(&a, 0, sizeof(a));
-                a.o = u.o; a.n = u.n; a.npos = n; a.lend = o + cnt; a.lbeg = o;
-                a.halo = Ld > min_d ? halo : nullptr;
+                a.o = u.o; a.n = u.n; a.npos = n; a.lend = o + cnt;
                 a.nb = nb; a.uv = uv; a.bar = bar; a.P4 = P4; a.Q4 = Q4; a.Q1 = Q1; a.dat = dat; a.snap = snap;
                 a.lid = lid; a.acc = acc; a.done = done; a.slot0 = u.slot;
                 a.alpha0 = prm->alpha0; a.alpha1 = prm->alpha1;
@@ -3108,7 +3051,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         std::memcpy(&fb[2], &prm->tol, 4);
         for (uint32_t f : fb) key.push_back(f);
         const FuseSet& fz0 = fsets[levels.front().d];
-        const void* ptrs[] = {nb, par, uv, bar, P4, Q4, Q1, dat, snap, lid, acc, flags, resid, lv_res, halo,
+        const void* ptrs[] = {nb, par, uv, bar, P4, Q4, Q1, dat, snap, lid, acc, flags, resid, lv_res,
                               fused_ok ? fz0.barB : nullptr, fused_ok ? fz0.P4B : nullptr,
                               fused_ok ? fz0.Q4B : nullptr, fused_ok ? fz0.Q1B : nullptr,
                               fused_ok ? fz0.slot : nullptr, fused_ok ? fz0.halo : nullptr};
