@@ -2507,12 +2507,18 @@ static int run_unit_t(tgvg_ctx* ctx, IterArgs& a, int iters, bool stop, bool tim
             TGVG_CK(ctx, cudaEventSynchronize(ctx->ev[3]));
             it += TUNE_SEG;
             if (stop) {
-                // A unit that met its tolerance during the trials is finished: its
-                // last segment stopped early, so nothing is recorded for the class.
+                // A unit that met its tolerance during the trials is finished.  Its
+                // last segment stopped early and is not compared; the class keeps the
+                // fastest complete trial (or this candidate when there is none), so
+                // that later units of the class do not pay for the trials again.
                 TGVG_CK(ctx, cudaMemcpy(done_h.data(), a.done + a.slot0, sizeof(int) * ns, cudaMemcpyDeviceToHost));
                 bool all = true;
                 for (int d : done_h) all = all && d != 0;
-                if (all) { *used = effective_cfg<MODE>(ctx, c, a.n); return TGVG_OK; }
+                if (all) {
+                    ctx->tune[MODE][31 - __builtin_clz((unsigned)std::max(1, a.n))] = best_ms < 1e30f ? best : c;
+                    *used = effective_cfg<MODE>(ctx, c, a.n);
+                    return TGVG_OK;
+                }
             }
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
