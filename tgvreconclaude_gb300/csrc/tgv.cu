@@ -367,6 +367,7 @@ struct IterArgs {
     int swap;             // per-launch schedules: dual sweep in reverse order, primal forward
     int band;             // per-launch schedules: warps stride over the whole unit (grid-stride band)
     int lend;             // end of the level's positions; cubes at lend and beyond are deeper
+    int gcap;             // single-block shared-memory schedule: room for staged out-of-unit values
 };
 
 // Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
@@ -1072,6 +1073,8 @@ __device__ __forceinline__ void dual_res(const DualLd& L, const float4& Po, cons
 // split kernels' (dual_math, primal_math).
 constexpr int SMEM_MAX_N = 2048;
 static inline size_t smem_level_bytes(int n) { return size_t(n) * 100; }
+// Staged out-of-unit values follow the unit's arrays at a 16-byte boundary.
+static inline size_t smem_ghost_offset(int n) { return (smem_level_bytes(n) + 15) & ~size_t(15); }
 
 template <int MODE>
 __device__ __forceinline__ float4 smem_bar(const IterArgs& a, const float4* s_bar, int j, const float4& own) {
@@ -1103,12 +1106,43 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_smem(IterArgs a) {
     float2* s_dat = reinterpret_cast<float2*>(s_Q + n);
     float* s_q5 = reinterpret_cast<float*>(s_dat + n);
     int* s_nb = reinterpret_cast<int*>(s_q5 + n);  // [6][n]
+    float4* s_gh = reinterpret_cast<float4*>(smem_raw + ((size_t(n) * 100 + 15) & ~size_t(15)));
+    __shared__ int s_ng;
+    if (threadIdx.x == 0) s_ng = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int p = o + i;
         s_uv[i] = a.uv[p]; s_bar[i] = a.bar[p]; s_P[i] = a.P4[p]; s_Q[i] = a.Q4[p];
         s_dat[i] = a.dat[p]; s_q5[i] = a.Q1[p];
 #pragma unroll
         for (int f = 0; f < 6; ++f) s_nb[f * n + i] = a.nb[(size_t)f * a.npos + p];
+    }
+    __syncthreads();
+    // Cubes outside the unit (coarser and deeper levels, other leaves, the
+    // snapshot) do not change during the launch: the values a face reads from
+    // one are staged once, so the iterations touch only shared memory.  A
+    // staged face holds slot -2 - g of s_gh: the neighbour's bars for the dual
+    // faces +x/+y/+z, the four gathered p/q values for the primal faces
+    // -x/-y/-z.  Faces beyond the room left in shared memory keep reading
+    // global memory.
+    for (int idx = threadIdx.x; idx < 6 * n; idx += blockDim.x) {
+        const int f = idx / n;
+        const int j = s_nb[idx];
+        if (j < 0) continue;
+        const bool border = MODE != M_INMEM && (j & BORDER);
+        const int jj = j & POS_MASK;
+        if (!border && (unsigned)(jj - o) < (unsigned)n) continue;  // inside the unit
+        if ((f & 1) && MODE == M_STREAM && border) continue;         // reads as zero already
+        float4 g;
+        if (!(f & 1)) {
+            g = border ? a.snap[jj] : a.bar[jj];
+        } else {
+            const float4 A = a.P4[jj], B = a.Q4[jj];
+            const float c5 = a.Q1[jj];
+            g = f == 1 ? make_float4(A.x, A.w, B.z, B.w)
+              : f == 3 ? make_float4(A.y, B.x, B.z, c5) : make_float4(A.z, B.y, B.w, c5);
+        }
+        const int slot = atomicAdd(&s_ng, 1);
+        if (slot < a.gcap) { s_gh[slot] = g; s_nb[idx] = -2 - slot; }
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -1127,9 +1161,10 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_smem(IterArgs a) {
             if (work) {
                 DualLd L;
                 L.b = s_bar[i]; L.P = s_P[i]; L.Q = s_Q[i]; L.q5 = s_q5[i];
-                L.B0 = smem_bar<MODE>(a, s_bar, s_nb[i], L.b);
-                L.B2 = smem_bar<MODE>(a, s_bar, s_nb[2 * n + i], L.b);
-                L.B4 = smem_bar<MODE>(a, s_bar, s_nb[4 * n + i], L.b);
+                const int j0 = s_nb[i], j2 = s_nb[2 * n + i], j4 = s_nb[4 * n + i];
+                L.B0 = j0 <= -2 ? s_gh[-2 - j0] : smem_bar<MODE>(a, s_bar, j0, L.b);
+                L.B2 = j2 <= -2 ? s_gh[-2 - j2] : smem_bar<MODE>(a, s_bar, j2, L.b);
+                L.B4 = j4 <= -2 ? s_gh[-2 - j4] : smem_bar<MODE>(a, s_bar, j4, L.b);
                 float4 Po, Qo;
                 float q5n;
                 dual_math(a, L, Po, Qo, q5n);
@@ -1155,13 +1190,23 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_smem(IterArgs a) {
                 L.gp52 = L.gq52 = L.gq54 = L.gq55 = 0.f;
                 float4 A, B;
                 float c5;
-                if (smem_pq<MODE>(a, s_P, s_Q, s_q5, s_nb[n + i], A, B, c5)) {
+                const int j1 = s_nb[n + i], j3 = s_nb[3 * n + i], j5 = s_nb[5 * n + i];
+                if (j1 <= -2) {
+                    const float4 g = s_gh[-2 - j1];
+                    L.gp10 = g.x; L.gq10 = g.y; L.gq13 = g.z; L.gq14 = g.w;
+                } else if (smem_pq<MODE>(a, s_P, s_Q, s_q5, j1, A, B, c5)) {
                     L.gp10 = A.x; L.gq10 = A.w; L.gq13 = B.z; L.gq14 = B.w;
                 }
-                if (smem_pq<MODE>(a, s_P, s_Q, s_q5, s_nb[3 * n + i], A, B, c5)) {
+                if (j3 <= -2) {
+                    const float4 g = s_gh[-2 - j3];
+                    L.gp31 = g.x; L.gq31 = g.y; L.gq33 = g.z; L.gq35 = g.w;
+                } else if (smem_pq<MODE>(a, s_P, s_Q, s_q5, j3, A, B, c5)) {
                     L.gp31 = A.y; L.gq31 = B.x; L.gq33 = B.z; L.gq35 = c5;
                 }
-                if (smem_pq<MODE>(a, s_P, s_Q, s_q5, s_nb[5 * n + i], A, B, c5)) {
+                if (j5 <= -2) {
+                    const float4 g = s_gh[-2 - j5];
+                    L.gp52 = g.x; L.gq52 = g.y; L.gq54 = g.z; L.gq55 = g.w;
+                } else if (smem_pq<MODE>(a, s_P, s_Q, s_q5, j5, A, B, c5)) {
                     L.gp52 = A.z; L.gq52 = B.y; L.gq54 = B.w; L.gq55 = c5;
                 }
                 float4 uvn, barn;
@@ -2088,7 +2133,12 @@ static int effective_cfg(const tgvg_ctx* ctx, int cfg, int n) {
 template <int MODE>
 static int smem_level_setup(tgvg_ctx* ctx) {
     if (ctx->smem_level_ready[MODE]) return TGVG_OK;
-    const int bytes = (int)smem_level_bytes(SMEM_MAX_N);
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) != cudaSuccess)
+        return ctx->cuda_fail(cudaGetLastError(), "shared memory opt-in limit");
+    // the unit's arrays at the largest unit size, plus what is left for staged values
+    const int bytes = std::max((int)smem_ghost_offset(SMEM_MAX_N), optin - 1024);
+    ctx->smem_level_max = bytes;
     cudaError_t e = cudaFuncSetAttribute((const void*)k_level_smem<MODE, false>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
@@ -2312,7 +2362,9 @@ static int run_segment(tgvg_ctx* ctx, IterArgs a, int cfg, int it0, int count, b
         if (rc) return rc;
         a.it0 = it0;
         a.iters = count;
-        const size_t sh = smem_level_bytes(a.n);
+        const size_t base = smem_ghost_offset(a.n);
+        const size_t sh = std::min((size_t)ctx->smem_level_max, base + size_t(16) * 6 * a.n);
+        a.gcap = (int)((sh - base) / 16);
         if (stop) k_level_smem<MODE, true><<<1, CLUSTER_BLOCK, sh, ctx->stream>>>(a);
         else k_level_smem<MODE, false><<<1, CLUSTER_BLOCK, sh, ctx->stream>>>(a);
         TGVG_LAUNCHED(ctx);
