@@ -191,6 +191,7 @@ extern "C" int tgvg_create(int device, tgvg_ctx** out) {
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
     for (auto& e : c->lev_ev) cudaEventCreate(&e);
+    for (auto& e : c->chk_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     level_thresholds(c->lvl_thresh);
     *out = c;
     return TGVG_OK;
@@ -207,6 +208,8 @@ extern "C" int tgvg_destroy(tgvg_ctx* ctx) {
         for (auto& e : ctx->ev) cudaEventDestroy(e);
         for (auto& e : ctx->tev) cudaEventDestroy(e);
         for (auto& e : ctx->lev_ev) cudaEventDestroy(e);
+        for (auto& e : ctx->chk_ev) cudaEventDestroy(e);
+        if (ctx->chk_host) cudaFreeHost(ctx->chk_host);
         if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
         cudaStreamDestroy(ctx->stream);
     }

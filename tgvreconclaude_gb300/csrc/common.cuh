@@ -190,6 +190,9 @@ struct tgvg_ctx {
     int wave_occ[3][2] = {};           // blocks/SM of the wavefront kernel per mode [L2 loads, L1 loads]
     bool smem_level_ready[3] = {};     // shared-memory limit of the tiny-level kernel raised, per mode
     int smem_level_max = 0;            // dynamic shared memory that kernel may use (bytes)
+    cudaEvent_t chk_ev[2] = {};        // stopping flags copied back while the next chunk of iterations runs
+    int* chk_host = nullptr;           // pinned host copies of those flags (2 x chk_cap)
+    int chk_cap = 0;
     int dsm_max[3] = {-1, -1, -1};     // cluster size of the distributed-shared-memory kernel per mode (-1 unknown)
     cudaEvent_t lev_ev[2 * TGVG_MAX_LEVELS] = {};  // per-level start/end
     bool graphs = true;                // capture the level loop into a CUDA graph when possible

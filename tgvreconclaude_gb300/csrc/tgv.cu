@@ -2584,7 +2584,41 @@ static int run_unit_t(tgvg_ctx* ctx, IterArgs& a, int iters, bool stop, bool tim
         if ((rc = dsm_capacity<MODE>(ctx, &cs))) return rc;
     }
     *used = effective_cfg<MODE>(ctx, cfg, a.n);
-    return run_segment<MODE>(ctx, a, cfg, it, iters - it, stop, timed);
+    const int eff = *used;
+    if (!stop || ctx->capturing || !(per_launch_cfg(eff) || fused_cfg(eff) || wave_cfg(eff)))
+        return run_segment<MODE>(ctx, a, cfg, it, iters - it, stop, timed);
+    // A tolerance-stopped unit on a schedule with launches per iteration: its
+    // launches after convergence would return at once but still cost a launch
+    // each (at a 6000-iteration cap, about 20 ms).  So the iterations are
+    // enqueued in chunks of growing length, and each chunk's stopping flags are
+    // copied back while the next chunk runs; once they show the unit finished,
+    // nothing more is enqueued.  At most one chunk runs after convergence.
+    const int ns = unit_slots<MODE>(a.nslot);
+    if (ctx->chk_cap < ns) {
+        if (ctx->chk_host) cudaFreeHost(ctx->chk_host);
+        ctx->chk_host = nullptr;
+        ctx->chk_cap = 0;
+        TGVG_CK(ctx, cudaHostAlloc((void**)&ctx->chk_host, sizeof(int) * 2 * ns, cudaHostAllocDefault));
+        ctx->chk_cap = ns;
+    }
+    int seg = 64;
+    for (int k = 0; it < iters; ++k) {
+        const int cnt = std::min(seg, iters - it);
+        if ((rc = run_segment<MODE>(ctx, a, cfg, it, cnt, stop, timed))) return rc;
+        it += cnt;
+        int* h = ctx->chk_host + (k & 1) * ns;
+        TGVG_CK(ctx, cudaMemcpyAsync(h, a.done + a.slot0, sizeof(int) * ns, cudaMemcpyDeviceToHost, ctx->stream));
+        TGVG_CK(ctx, cudaEventRecord(ctx->chk_ev[k & 1], ctx->stream));
+        if (k > 0) {
+            TGVG_CK(ctx, cudaEventSynchronize(ctx->chk_ev[(k - 1) & 1]));
+            const int* hp = ctx->chk_host + ((k - 1) & 1) * ns;
+            bool all = true;
+            for (int s = 0; s < ns && all; ++s) all = hp[s] != 0;
+            if (all) break;
+        }
+        seg = std::min(seg * 2, 1024);
+    }
+    return TGVG_OK;
 }
 
 static int plan_unit(tgvg_ctx* ctx, int mode, int n, int iters, bool stop, bool timed, int* cfg) {
