@@ -23,11 +23,16 @@
 
 namespace tgvg {
 
-struct DevCam {
-    long long base;   // element offset of level 0 in the texel buffer
+// Laid out so that the fields the binning loop reads for every pair come as
+// five 16-byte shared-memory loads: the three rows of Rt_inv, (fx, fy, cx, cy)
+// and (|fx|, W, H, nlev).
+struct __align__(16) DevCam {
     float m[12];      // rows 0..2 of Rt_inv (row-major)
-    float fx, fy, cx, cy, absfx;
-    int W, H, nlev, vote;
+    float fx, fy, cx, cy;
+    float absfx;
+    int W, H, nlev;
+    long long base;   // element offset of level 0 in the texel buffer
+    int vote;
     int off[13];      // element offset of level l relative to base
 };
 static_assert(sizeof(DevCam) == 144, "DevCam layout");
@@ -260,22 +265,25 @@ k_histograms(const uint4* __restrict__ cubes, int64_t n, const DevCam* __restric
         for (int cc = 0; cc < nb; ++cc) {
             if (!s_vis[cc]) continue;  // block-uniform: no centre of the block can pass project()
             const DevCam& c = s_cam[cc];
+            const float4* c4 = reinterpret_cast<const float4*>(&c);
+            const float4 r0 = c4[0], r1 = c4[1], r2 = c4[2], k4 = c4[3], e4 = c4[4];
+            const int cW = __float_as_int(e4.y), cH = __float_as_int(e4.z), cL = __float_as_int(e4.w);
             // project (histogram.cpp:76-106): cam = Rt_inv * [P, 1]
-            float X = fmul(c.m[0], px); X = fadd(X, fmul(c.m[1], py)); X = fadd(X, fmul(c.m[2], pz));
-            X = fadd(X, fmul(c.m[3], 1.0f));
-            float Y = fmul(c.m[4], px); Y = fadd(Y, fmul(c.m[5], py)); Y = fadd(Y, fmul(c.m[6], pz));
-            Y = fadd(Y, fmul(c.m[7], 1.0f));
-            float Z = fmul(c.m[8], px); Z = fadd(Z, fmul(c.m[9], py)); Z = fadd(Z, fmul(c.m[10], pz));
-            Z = fadd(Z, fmul(c.m[11], 1.0f));
+            float X = fmul(r0.x, px); X = fadd(X, fmul(r0.y, py)); X = fadd(X, fmul(r0.z, pz));
+            X = fadd(X, fmul(r0.w, 1.0f));
+            float Y = fmul(r1.x, px); Y = fadd(Y, fmul(r1.y, py)); Y = fadd(Y, fmul(r1.z, pz));
+            Y = fadd(Y, fmul(r1.w, 1.0f));
+            float Z = fmul(r2.x, px); Z = fadd(Z, fmul(r2.y, py)); Z = fadd(Z, fmul(r2.z, pz));
+            Z = fadd(Z, fmul(r2.w, 1.0f));
             if (Z <= 0.0f) continue;
-            const float u_f = fadd(fmul(fdiv(X, Z), c.fx), c.cx);
-            const float v_f = fadd(fmul(fdiv(Y, Z), c.fy), c.cy);
+            const float u_f = fadd(fmul(fdiv(X, Z), k4.x), k4.z);
+            const float v_f = fadd(fmul(fdiv(Y, Z), k4.y), k4.w);
             const int u0 = trunc_i32(u_f), v0 = trunc_i32(v_f);
-            if (u0 < 0 || u0 >= c.W || v0 < 0 || v0 >= c.H) continue;
+            if (u0 < 0 || u0 >= cW || v0 < 0 || v0 >= cH) continue;
             // level = clamp((int)log2(max(1, |fx| r_c / z)), 0, L-1) through the
             // host-computed thresholds of (int)log2f; +inf gives level 0 as the
             // reference's int conversion of log2f(inf) does on x86-64.
-            const float fp = fdiv(fmul(c.absfx, r_c), Z);
+            const float fp = fdiv(fmul(e4.x, r_c), Z);
             const float xm = (1.0f < fp) ? fp : 1.0f;
             int lv = 0;
             if (xm < INFINITY) {
@@ -287,8 +295,8 @@ k_histograms(const uint4* __restrict__ cubes, int64_t n, const DevCam* __restric
                     for (int k = 1; k < 13; ++k) lv += (xm >= s_thr[k]) ? 1 : 0;
                 }
             }
-            lv = min(lv, c.nlev - 1);
-            const int lw = max(1, c.W >> lv), lh = max(1, c.H >> lv);
+            lv = min(lv, cL - 1);
+            const int lw = max(1, cW >> lv), lh = max(1, cH >> lv);
             int uu = u0 >> lv, vv = v0 >> lv;
             uu = uu < 0 ? 0 : (lw - 1 < uu ? lw - 1 : uu);
             vv = vv < 0 ? 0 : (lh - 1 < vv ? lh - 1 : vv);
