@@ -359,10 +359,11 @@ static void run_level(const std::vector<uint32_t>& act, const std::vector<int32_
             for (int k = 0; k < 6; ++k) { q_old[k] = st[i].q[k]; st[i].q[k] += sigma * e[k]; }
             clip6(st[i].q, alpha0);
             if (check) {
-                double d = 0;
-                for (int k = 0; k < 3; ++k) { double t = double(st[i].p[k]) - double(p_old[k]); d += t * t; }
-                for (int k = 0; k < 6; ++k) { double t = double(st[i].q[k]) - double(q_old[k]); d += t * t; }
-                ddual += d;
+                // per-cube terms in S, in component order; sums over cubes in FP64
+                S d = S(0);
+                for (int k = 0; k < 3; ++k) { S t = st[i].p[k] - p_old[k]; d = d + t * t; }
+                for (int k = 0; k < 6; ++k) { S t = st[i].q[k] - q_old[k]; d = d + t * t; }
+                ddual += double(d);
             }
         }
         // The p and q sweeps of the reference are separate loops; fusing them per
@@ -386,15 +387,18 @@ static void run_level(const std::vector<uint32_t>& act, const std::vector<int32_
         for (int64_t a = 0; a < na; ++a) {
             const uint32_t i = act[a];
             if (check) {
-                double t0 = double(un[a]) - double(st[i].u), t1 = double(vxn[a]) - double(st[i].v[0]);
-                double t2 = double(vyn[a]) - double(st[i].v[1]), t3 = double(vzn[a]) - double(st[i].v[2]);
-                dprim += t0 * t0 + t1 * t1 + t2 * t2 + t3 * t3;
-                nprim += double(un[a]) * un[a] + double(vxn[a]) * vxn[a] + double(vyn[a]) * vyn[a] +
-                         double(vzn[a]) * vzn[a];
-                double nd = 0;
-                for (int k = 0; k < 3; ++k) nd += double(st[i].p[k]) * st[i].p[k];
-                for (int k = 0; k < 6; ++k) nd += double(st[i].q[k]) * st[i].q[k];
-                ndual += nd;
+                const S t0 = un[a] - st[i].u, t1 = vxn[a] - st[i].v[0];
+                const S t2 = vyn[a] - st[i].v[1], t3 = vzn[a] - st[i].v[2];
+                S dp = t0 * t0;
+                dp = dp + t1 * t1; dp = dp + t2 * t2; dp = dp + t3 * t3;
+                dprim += double(dp);
+                S np = un[a] * un[a];
+                np = np + vxn[a] * vxn[a]; np = np + vyn[a] * vyn[a]; np = np + vzn[a] * vzn[a];
+                nprim += double(np);
+                S nd = S(0);
+                for (int k = 0; k < 3; ++k) nd = nd + st[i].p[k] * st[i].p[k];
+                for (int k = 0; k < 6; ++k) nd = nd + st[i].q[k] * st[i].q[k];
+                ndual += double(nd);
             }
             ub[i] = S(2) * un[a] - st[i].u;
             vbx[i] = S(2) * vxn[a] - st[i].v[0];

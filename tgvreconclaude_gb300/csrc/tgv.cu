@@ -470,6 +470,26 @@ __device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const floa
     return ld4<CG>(bar + j);
 }
 
+// One cube's terms of the stopping test: the squared change and the squared
+// new value of its K state components, each summed in FP32 with explicit
+// rounding in component order (the oracle sums them the same way); the sums
+// over cubes are FP64.  GB300's FP64 rate is a small fraction of its FP32
+// rate: with the per-cube terms in FP64 a checking iteration cost 3.6 times
+// a plain one on the largest levels.
+template <int K>
+__device__ __forceinline__ void res_terms(const float* w, const float* o, double& dd, double& nd) {
+    float t = fsub(w[0], o[0]);
+    float ds = fmul(t, t), ns = fmul(w[0], w[0]);
+#pragma unroll
+    for (int k = 1; k < K; ++k) {
+        t = fsub(w[k], o[k]);
+        ds = fadd(ds, fmul(t, t));
+        ns = fadd(ns, fmul(w[k], w[k]));
+    }
+    dd = (double)ds;
+    nd = (double)ns;
+}
+
 // One cube's dual ascent: p on |grad u - v| (radius alpha1) and q on |e(v)|
 // (radius alpha0), in the reference's operation order (tgv.cpp:158-189).
 // Split into the loads (dual_load) and the arithmetic and stores (dual_finish)
@@ -511,13 +531,9 @@ __device__ __forceinline__ void dual_finish(const IterArgs& a, int p, const Dual
     st4L(a.Q4 + p, make_float4(q[1], q[2], q[3], q[4]), pol);
     st1L(a.Q1 + p, q[5], pol);
     if (RES) {
-        const double d0 = (double)p0 - P.x, d1 = (double)p1 - P.y, d2 = (double)p2 - P.z;
-        const double d3 = (double)q[0] - P.w, d4 = (double)q[1] - Q.x, d5 = (double)q[2] - Q.y;
-        const double d6 = (double)q[3] - Q.z, d7 = (double)q[4] - Q.w, d8 = (double)q[5] - q5o;
-        dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5 + d6 * d6 + d7 * d7 + d8 * d8;
-        nd = (double)p0 * p0 + (double)p1 * p1 + (double)p2 * p2;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) nd += (double)q[k] * q[k];
+        const float o[9] = {P.x, P.y, P.z, P.w, Q.x, Q.y, Q.z, Q.w, q5o};
+        const float w[9] = {p0, p1, p2, q[0], q[1], q[2], q[3], q[4], q[5]};
+        res_terms<9>(w, o, dd, nd);
     }
 }
 
@@ -621,9 +637,9 @@ __device__ __forceinline__ void primal_math(const PrimalLd& L, float4& uvn, floa
                        fsub(fmul(2.0f, vzn), U.w));
     uvn = make_float4(un, vxn, vyn, vzn);
     if (RES) {
-        const double d0 = (double)un - U.x, d1 = (double)vxn - U.y, d2 = (double)vyn - U.z, d3 = (double)vzn - U.w;
-        dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
-        nd = (double)un * un + (double)vxn * vxn + (double)vyn * vyn + (double)vzn * vzn;
+        const float o[4] = {U.x, U.y, U.z, U.w};
+        const float w[4] = {un, vxn, vyn, vzn};
+        res_terms<4>(w, o, dd, nd);
     }
 }
 
@@ -1092,12 +1108,9 @@ __device__ __forceinline__ void dual_math(const IterArgs& a, const DualLd& L, fl
 // FP64 residual terms of one dual update (as dual_finish computes them).
 __device__ __forceinline__ void dual_res(const DualLd& L, const float4& Po, const float4& Qo, float q5n, double& dd,
                                          double& nd) {
-    const double d0 = (double)Po.x - L.P.x, d1 = (double)Po.y - L.P.y, d2 = (double)Po.z - L.P.z;
-    const double d3 = (double)Po.w - L.P.w, d4 = (double)Qo.x - L.Q.x, d5 = (double)Qo.y - L.Q.y;
-    const double d6 = (double)Qo.z - L.Q.z, d7 = (double)Qo.w - L.Q.w, d8 = (double)q5n - L.q5;
-    dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5 + d6 * d6 + d7 * d7 + d8 * d8;
-    nd = (double)Po.x * Po.x + (double)Po.y * Po.y + (double)Po.z * Po.z + (double)Po.w * Po.w +
-         (double)Qo.x * Qo.x + (double)Qo.y * Qo.y + (double)Qo.z * Qo.z + (double)Qo.w * Qo.w + (double)q5n * q5n;
+    const float o[9] = {L.P.x, L.P.y, L.P.z, L.P.w, L.Q.x, L.Q.y, L.Q.z, L.Q.w, L.q5};
+    const float w[9] = {Po.x, Po.y, Po.z, Po.w, Qo.x, Qo.y, Qo.z, Qo.w, q5n};
+    res_terms<9>(w, o, dd, nd);
 }
 
 // ---- tiny levels in shared memory (schedule 23) -------------------------------
