@@ -723,7 +723,10 @@ __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpA
             work[u] = gu < ngroups && pos[u] < end;
             slot[u] = -1;
             if (work[u]) slot[u] = (MODE == M_STREAM) ? __ldg(a.lid + pos[u]) : a.slot0;
-            if (STOP && work[u] && MODE == M_STREAM) work[u] = __ldcg(a.done + slot[u]) == 0;
+            // The stopping flags change only between launches of the per-launch
+            // schedules (k_check is its own launch), so they are read through L1
+            // there; the one-launch schedules re-read them from L2.
+            if (STOP && work[u] && MODE == M_STREAM) work[u] = (CG ? __ldcg(a.done + slot[u]) : __ldg(a.done + slot[u])) == 0;
         }
         if (DUAL) {
             DualLd L[ILP];
@@ -1464,7 +1467,7 @@ __global__ void __launch_bounds__(FT) k_fused(IterArgs a, FuseArgs f) {
         bool own = p < a.o + a.n;
         int slot = -1;
         if (own) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
-        if (STOP && own && MODE == M_STREAM) own = __ldcg(a.done + slot) == 0;
+        if (STOP && own && MODE == M_STREAM) own = __ldg(a.done + slot) == 0;
         // dual: the tile's own cubes
         double dd = 0.0, nd = 0.0;
         if (own) {
@@ -1658,7 +1661,7 @@ __global__ void __launch_bounds__(FT) k_fused_tma(IterArgs a, FuseArgs f) {
         bool own = threadIdx.x < cnt;
         int slot = -1;
         if (own) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
-        if (STOP && own && MODE == M_STREAM) own = __ldcg(a.done + slot) == 0;
+        if (STOP && own && MODE == M_STREAM) own = __ldg(a.done + slot) == 0;
         // offsets of the 4- and 8-byte slices inside their stage arrays
         int oq1, onb[3], osl[3], odat;
         slice_bytes(f.Q1_r + t0, 4, cnt, oq1);
@@ -1850,7 +1853,7 @@ __device__ __forceinline__ int wave_cube(const IterArgs& a, const WaveArgs& w, i
     work = p >= a.o && p < a.o + a.n;
     slot = -1;
     if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
-    if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
+    if (STOP && work && MODE == M_STREAM) work = __ldg(a.done + slot) == 0;
     return p;
 }
 
