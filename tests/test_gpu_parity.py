@@ -352,6 +352,36 @@ def test_tgv_stopping_rule(oracle_lib):
         assert_state_equal(out, ref, f"stop {mode}")
 
 
+def test_stream_leaves_stop_apart_within_a_level(oracle_lib):
+    """Streaming semantics, per-launch schedules: within one level some leaves
+    meet the tolerance while another runs to the cap (its cubes have no votes, so
+    the reference iteration drifts), and on shallow levels some leaves have no
+    cube at all.  The sweep kernels skip the per-cube stopping-flag reads until a
+    leaf of the level has met the tolerance; states and iteration counts must
+    still equal the oracle's on every level."""
+    ctx = api.context()
+    rng = np.random.default_rng(52)
+    cubes = S.random_octree(rng, dmin=2, dmax=7, target=30000, shape="sphere")
+    hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.0)
+    leaves = S.split_leaves(len(cubes), 6, rng, cubes, aligned=True)
+    f, l = int(leaves["first_idx"][0]), int(leaves["last_idx"][0])
+    hists[f:l + 1] = 0
+    ref, rst = oracle_lib.tgv_solve(cubes, hists, leaves, "stream", 2.0, 1.0, 600, tol=1e-3, check_every=10,
+                                    nthreads=8)
+    its = [r["iters_run"] for r in rst]
+    assert 600 in its and min(its) < 600
+    try:
+        for cfg in (0, 7, 8, 12, 14, 16, 18):
+            ctx.set_schedule("stream", -1, cfg)
+            out, st = api.tgv_solve(cubes, hists, leaves, "stream",
+                                    api.TGVParams(alpha0=2.0, alpha1=1.0, iters=600, tol=1e-3, check_every=10))
+            assert set(st["schedule"]) == {cfg}
+            assert_state_equal(out, ref, f"schedule {cfg} leaves stopping apart")
+            assert st["iters_run"] == its, cfg
+    finally:
+        ctx.set_schedule("stream", -1, -1)
+
+
 @pytest.mark.parametrize("mode", ["inmem", "stream"])
 def test_tgv_autotuned_stopping_solves(oracle_lib, mode):
     """Tolerance-stopped solves with a large iteration cap tune their untuned

@@ -696,8 +696,10 @@ __device__ __forceinline__ void prefetch_group(const IterArgs& a, int q0, int en
 // With ILP = 2 a warp takes two of its groups per step and issues the loads
 // of both cubes before either's arithmetic and stores (more loads in flight
 // per warp at the same occupancy).
+// chk = false (streaming semantics, per-launch schedules): no slot of the unit
+// has met its tolerance, so no cube reads its slot's stopping flag.
 template <int MODE, bool RES, bool STOP, bool CG, bool DUAL, bool REV, int ILP = 1>
-__device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpAcc& wa) {
+__device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpAcc& wa, bool chk = true) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int g0 = warp, gs = blockDim.x >> 5;
     if (!CG && a.band) {
@@ -722,11 +724,13 @@ __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpA
             pos[u] = beg + g * 32 + lane;
             work[u] = gu < ngroups && pos[u] < end;
             slot[u] = -1;
-            if (work[u]) slot[u] = (MODE == M_STREAM) ? __ldg(a.lid + pos[u]) : a.slot0;
+            if (work[u] && (MODE != M_STREAM || RES || (STOP && chk)))
+                slot[u] = (MODE == M_STREAM) ? __ldg(a.lid + pos[u]) : a.slot0;
             // The stopping flags change only between launches of the per-launch
             // schedules (k_check is its own launch), so they are read through L1
             // there; the one-launch schedules re-read them from L2.
-            if (STOP && work[u] && MODE == M_STREAM) work[u] = (CG ? __ldcg(a.done + slot[u]) : __ldg(a.done + slot[u])) == 0;
+            if (STOP && chk && work[u] && MODE == M_STREAM)
+                work[u] = (CG ? __ldcg(a.done + slot[u]) : __ldg(a.done + slot[u])) == 0;
         }
         if (DUAL) {
             DualLd L[ILP];
@@ -758,15 +762,40 @@ __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpA
 // order so it starts on the cubes whose p/q the dual sweep wrote last.
 // MINB = 8 caps registers at 32 so that 64 warps fit per SM (more loads in
 // flight); MINB = 6 (the default) allows about 42.
+// Streaming semantics: the block first reads the unit's stopping flags (they
+// change only between launches).  All set: nothing to do.  None set by a met
+// tolerance (a slot with no cube on the level holds 2, not 1): no cube needs its
+// own flag, which saves each cube a dependent read of its slot and flag before
+// its loads.  Units with more slots than this bound keep the per-cube reads.
+constexpr int STOP_SCAN_MAX = 4 * ITER_BLOCK;
+template <int MODE, bool STOP>
+__device__ __forceinline__ bool unit_flags(const IterArgs& a, bool& chk) {
+    chk = true;
+    if (!STOP) return true;
+    if (MODE != M_STREAM) return a.done[a.slot0] == 0;
+    if (a.nslot > STOP_SCAN_MAX) return true;
+    int any = 0, all = 1;
+    for (int s = threadIdx.x; s < a.nslot; s += blockDim.x) {
+        const int d = __ldg(a.done + a.slot0 + s);
+        any |= d == 1;
+        all &= d != 0;
+    }
+    any = __syncthreads_or(any);
+    all = __syncthreads_and(all);
+    chk = any != 0;
+    return all == 0;
+}
+
 template <int MODE, bool RES, bool STOP, int MINB, int ILP = 1>
 __global__ void __launch_bounds__(ITER_BLOCK, MINB) k_dual(IterArgs a) {
     pdl_wait();
     pdl_release();
-    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
+    bool chk;
+    if (!unit_flags<MODE, STOP>(a, chk)) return;
     const int beg = a.o + blockIdx.x * a.chunk;
     const int end = min(a.o + a.n, beg + a.chunk);
     WarpAcc wa;
-    sweep<MODE, RES, STOP, false, true, false, ILP>(a, beg, end, wa);
+    sweep<MODE, RES, STOP, false, true, false, ILP>(a, beg, end, wa, chk);
     if (RES) wa.flush(a.acc, 1, threadIdx.x & 31);
 }
 
@@ -774,12 +803,13 @@ template <int MODE, bool RES, bool STOP, int MINB, int ILP = 1>
 __global__ void __launch_bounds__(ITER_BLOCK, MINB) k_primal(IterArgs a) {
     pdl_wait();
     pdl_release();
-    if (MODE != M_STREAM && STOP && a.done[a.slot0]) return;
+    bool chk;
+    if (!unit_flags<MODE, STOP>(a, chk)) return;
     const int blk = gridDim.x - 1 - blockIdx.x;
     const int beg = a.o + blk * a.chunk;
     const int end = min(a.o + a.n, beg + a.chunk);
     WarpAcc wa;
-    sweep<MODE, RES, STOP, false, false, true, ILP>(a, beg, end, wa);
+    sweep<MODE, RES, STOP, false, false, true, ILP>(a, beg, end, wa, chk);
     if (RES) wa.flush(a.acc, 0, threadIdx.x & 31);
 }
 
@@ -959,6 +989,16 @@ __global__ void k_energy(int o, int cnt, int npos, const int* __restrict__ nb, c
     }
     for (int w = 16; w > 0; w >>= 1) e += __shfl_xor_sync(0xffffffffu, e, w);
     if ((threadIdx.x & 31) == 0 && e != 0.0) atomicAdd(out, e);
+}
+
+// Streaming semantics, tolerance-stopped solve: at each level's start a leaf's
+// stopping flag is 0 when the leaf has cubes on the level, else 2 (finished,
+// but not by a met tolerance, which sets 1).
+__global__ void k_done_init(int nleaf, int level, const int* __restrict__ ranges, int* __restrict__ done) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nleaf) return;
+    const int* r = ranges + (l * NBUCKET + level) * 2;
+    done[l] = r[1] > r[0] ? 0 : 2;
 }
 
 // Stopping test after a residual iteration: relative fixed-point residual
@@ -3134,7 +3174,12 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
             TGVG_LAUNCHED(ctx);
             if (stop) {
                 TGVG_CK(ctx, cudaMemsetAsync(acc, 0, 32ull * nslot, ctx->stream));
-                TGVG_CK(ctx, cudaMemsetAsync(done, 0, 4ull * nslot, ctx->stream));
+                if (mode == M_STREAM && L > 0) {
+                    k_done_init<<<blocks_for(L, 128), 128, 0, ctx->stream>>>(L, Ld, ranges, done);
+                    TGVG_LAUNCHED(ctx);
+                } else {
+                    TGVG_CK(ctx, cudaMemsetAsync(done, 0, 4ull * nslot, ctx->stream));
+                }
                 TGVG_CK(ctx, cudaMemsetAsync(resid, 0, 8ull * nslot, ctx->stream));
             }
             // NVTX range per level so profilers can select the largest level's launches
