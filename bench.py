@@ -163,13 +163,14 @@ def time_cpu_oracle(cubes, hists, iters, nthreads, repeats=1):
     oracle.build()
     best = None
     li = 0
+    out = None
     for _ in range(repeats):
         t0 = time.perf_counter()
-        _, st = oracle.tgv_solve(cubes, hists, None, "inmem", 2.0, 1.0, iters, nthreads=nthreads)
+        out, st = oracle.tgv_solve(cubes, hists, None, "inmem", 2.0, 1.0, iters, nthreads=nthreads)
         dt = time.perf_counter() - t0
         li = sum(s["active"] * s["iters_run"] for s in st)
         best = dt if best is None else min(best, dt)
-    return li / best, best, li
+    return li / best, best, li, out
 
 
 def run_reference(args):
@@ -204,12 +205,12 @@ def run_reference(args):
         time_cpu_oracle(cubes, hists, args.cpu_iters, threads)
     vals, tot_li, tot_t = [], 0, 0.0
     for _ in range(args.steps):
-        v, dt, li = time_cpu_oracle(cubes, hists, args.cpu_iters, threads)
+        v, dt, li, _ = time_cpu_oracle(cubes, hists, args.cpu_iters, threads)
         vals.append(v)
         tot_li += li
         tot_t += dt
     value = tot_li / tot_t
-    v1, dt1, _ = time_cpu_oracle(cubes, hists, args.cpu_iters, 1)
+    v1, dt1, _, _ = time_cpu_oracle(cubes, hists, args.cpu_iters, 1)
     sample = f"{len(cubes)} contiguous Morton-ordered cubes of {args.workload}, {args.cpu_iters} iterations per level, in-memory semantics, {threads} threads"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
@@ -625,7 +626,7 @@ def run_ours(args):
         cb, f64 = {}, {}
         if not args.skip_cpu:
             cubes_s, hists_s = cpu_sample(w, args.cpu_sample, args.cpu_iters)
-            v, dt, lis = time_cpu_oracle(cubes_s, hists_s, args.cpu_iters, 1)
+            v, dt, lis, ref32 = time_cpu_oracle(cubes_s, hists_s, args.cpu_iters, 1)
             cb = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "seconds": dt, "host_cores": os.cpu_count(),
                   "sample": f"{len(cubes_s)} contiguous Morton-ordered cubes of {args.workload}, {args.cpu_iters} iterations per "
                             f"level, in-memory semantics, single thread"}
@@ -638,7 +639,9 @@ def run_ours(args):
             bounded = np.abs(ref64[:, 0]) <= 1.0
             f64 = {"cubes": int(len(cubes_s)), "iters_per_level": args.cpu_iters, "max_abs_du": float(du.max()),
                    "rms_du": float(np.sqrt(np.mean(du ** 2))), "max_abs_du_bounded": float(du[bounded].max()),
-                   "what": "this package's FP32 u against the oracle's FP64 run on the same slice"}
+                   "what": "this package's FP32 u against the oracle's FP64 run on the same slice",
+                   "fp32_bit_exact": gpu32.tobytes() == ref32.tobytes(),
+                   "fp32_what": "the whole 13-float state against the oracle's FP32 run timed as cpu_baseline"}
 
         surf = {} if args.skip_surface else surface_eval(args, w, out_t)
         s13 = {} if args.skip_stages13 else stages13_eval(args, w)

@@ -370,33 +370,53 @@ struct IterArgs {
     int gcap;             // single-block shared-memory schedule: room for staged out-of-unit values
 };
 
-// Accumulate two FP64 values of the current 32-cube group into acc[slot*4+k0..]
-// with one atomic per warp per slot run (positions are sorted by leaf).
+// Error-free addition (Knuth's TwoSum, TAOCP vol. 2, 4.2.2): hi + x = s + e
+// exactly in round-to-nearest.  hi gets s and lo collects e, so (hi, lo) carries
+// a sum of FP32 terms to about 48 bits with FP32 arithmetic only.
+__device__ __forceinline__ void two_sum(float& hi, float& lo, float x) {
+    const float s = fadd(hi, x);
+    const float bp = fsub(s, hi);
+    const float e = fadd(fsub(hi, fsub(s, bp)), fsub(x, bp));
+    hi = s;
+    lo = fadd(lo, e);
+}
+
+// Accumulate two sums of per-cube FP32 terms over a warp's cubes of one slot,
+// and add them to acc[slot*4+k0..] in FP64 with one atomic per warp per slot
+// run (positions are sorted by leaf).  Within the warp the sums are two-term
+// floats: GB300's FP64 rate is a small fraction of its FP32 rate, and FP64
+// adds per cube made a checking iteration cost about twice a plain one on the
+// largest levels.  Only lane 0 converts to FP64, for the atomic.
 struct WarpAcc {
-    double x = 0.0, y = 0.0;
+    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f;
     int cur = -1;
     __device__ __forceinline__ void flush(double* acc, int k0, int lane) {
-        double a = x, b = y;
+        float ah = xh, al = xl, bh = yh, bl = yl;
         for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, o);
-            b += __shfl_xor_sync(0xffffffffu, b, o);
+            const float oah = __shfl_xor_sync(0xffffffffu, ah, o), oal = __shfl_xor_sync(0xffffffffu, al, o);
+            const float obh = __shfl_xor_sync(0xffffffffu, bh, o), obl = __shfl_xor_sync(0xffffffffu, bl, o);
+            two_sum(ah, al, oah);
+            al = fadd(al, oal);
+            two_sum(bh, bl, obh);
+            bl = fadd(bl, obl);
         }
         if (lane == 0 && cur >= 0) {
-            atomicAdd(acc + cur * 4 + k0, a);
-            atomicAdd(acc + cur * 4 + k0 + 2, b);
+            atomicAdd(acc + cur * 4 + k0, (double)ah + (double)al);
+            atomicAdd(acc + cur * 4 + k0 + 2, (double)bh + (double)bl);
         }
-        x = 0.0; y = 0.0;
+        xh = xl = yh = yl = 0.f;
     }
     // slot: this lane's slot (-1 if the lane has no cube); whole warp calls.
-    __device__ __forceinline__ void add(int slot, double dx, double dy, double* acc, int k0, int lane) {
+    __device__ __forceinline__ void add(int slot, float dx, float dy, double* acc, int k0, int lane) {
         const int s0 = __shfl_sync(0xffffffffu, slot, __ffs(__ballot_sync(0xffffffffu, slot >= 0)) - 1);
         const bool uniform = __all_sync(0xffffffffu, slot < 0 || slot == s0);
         if (uniform) {
             if (s0 != cur) { flush(acc, k0, lane); cur = s0; }
-            x += dx; y += dy;
+            two_sum(xh, xl, dx);
+            two_sum(yh, yl, dy);
         } else if (slot >= 0) {
-            atomicAdd(acc + slot * 4 + k0, dx);
-            atomicAdd(acc + slot * 4 + k0 + 2, dy);
+            atomicAdd(acc + slot * 4 + k0, (double)dx);
+            atomicAdd(acc + slot * 4 + k0 + 2, (double)dy);
         }
     }
 };
@@ -473,11 +493,12 @@ __device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const floa
 // One cube's terms of the stopping test: the squared change and the squared
 // new value of its K state components, each summed in FP32 with explicit
 // rounding in component order (the oracle sums them the same way); the sums
-// over cubes are FP64.  GB300's FP64 rate is a small fraction of its FP32
-// rate: with the per-cube terms in FP64 a checking iteration cost 3.6 times
-// a plain one on the largest levels.
+// over cubes are two-term floats within a warp and FP64 across warps (WarpAcc).
+// GB300's FP64 rate is a small fraction of its FP32 rate: with the per-cube
+// terms in FP64 a checking iteration cost 3.6 times a plain one on the largest
+// levels.
 template <int K>
-__device__ __forceinline__ void res_terms(const float* w, const float* o, double& dd, double& nd) {
+__device__ __forceinline__ void res_terms(const float* w, const float* o, float& dd, float& nd) {
     float t = fsub(w[0], o[0]);
     float ds = fmul(t, t), ns = fmul(w[0], w[0]);
 #pragma unroll
@@ -486,8 +507,8 @@ __device__ __forceinline__ void res_terms(const float* w, const float* o, double
         ds = fadd(ds, fmul(t, t));
         ns = fadd(ns, fmul(w[k], w[k]));
     }
-    dd = (double)ds;
-    nd = (double)ns;
+    dd = ds;
+    nd = ns;
 }
 
 // One cube's dual ascent: p on |grad u - v| (radius alpha1) and q on |e(v)|
@@ -510,7 +531,7 @@ __device__ __forceinline__ void dual_load(const IterArgs& a, int p, DualLd& L) {
 }
 
 template <bool RES>
-__device__ __forceinline__ void dual_finish(const IterArgs& a, int p, const DualLd& L, double& dd, double& nd) {
+__device__ __forceinline__ void dual_finish(const IterArgs& a, int p, const DualLd& L, float& dd, float& nd) {
     const float4 b = L.b, B0 = L.B0, B2 = L.B2, B4 = L.B4, P = L.P, Q = L.Q;
     const float q5o = L.q5;
     float p0 = fadd(P.x, fmul(0.25f, fsub(fsub(B0.x, b.x), b.y)));
@@ -538,7 +559,7 @@ __device__ __forceinline__ void dual_finish(const IterArgs& a, int p, const Dual
 }
 
 template <int MODE, bool RES, bool CG>
-__device__ __forceinline__ void dual_cube(const IterArgs& a, int p, double& dd, double& nd) {
+__device__ __forceinline__ void dual_cube(const IterArgs& a, int p, float& dd, float& nd) {
     DualLd L;
     dual_load<MODE, CG>(a, p, L);
     dual_finish<RES>(a, p, L, dd, nd);
@@ -610,7 +631,7 @@ __device__ __forceinline__ void primal_load(const IterArgs& a, int p, PrimalLd& 
 }
 
 template <bool RES>
-__device__ __forceinline__ void primal_math(const PrimalLd& L, float4& uvn, float4& barn, double& dd, double& nd) {
+__device__ __forceinline__ void primal_math(const PrimalLd& L, float4& uvn, float4& barn, float& dd, float& nd) {
     const float4 U = L.U, P = L.P, Q = L.Q;
     const float q5 = L.q5;
     const float2 D = L.D;
@@ -644,7 +665,7 @@ __device__ __forceinline__ void primal_math(const PrimalLd& L, float4& uvn, floa
 }
 
 template <bool RES>
-__device__ __forceinline__ void primal_finish(const IterArgs& a, int p, const PrimalLd& L, double& dd, double& nd) {
+__device__ __forceinline__ void primal_finish(const IterArgs& a, int p, const PrimalLd& L, float& dd, float& nd) {
     float4 uvn, barn;
     primal_math<RES>(L, uvn, barn, dd, nd);
     a.bar[p] = barn;
@@ -652,7 +673,7 @@ __device__ __forceinline__ void primal_finish(const IterArgs& a, int p, const Pr
 }
 
 template <int MODE, bool RES, bool CG>
-__device__ __forceinline__ void primal_cube(const IterArgs& a, int p, double& dd, double& nd) {
+__device__ __forceinline__ void primal_cube(const IterArgs& a, int p, float& dd, float& nd) {
     PrimalLd L;
     primal_load<MODE, CG>(a, p, L);
     primal_finish<RES>(a, p, L, dd, nd);
@@ -739,7 +760,7 @@ __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpA
                 if (work[u]) dual_load<MODE, CG>(a, pos[u], L[u]);
 #pragma unroll
             for (int u = 0; u < ILP; ++u) {
-                double dd = 0.0, nd = 0.0;
+                float dd = 0.f, nd = 0.f;
                 if (work[u]) dual_finish<RES>(a, pos[u], L[u], dd, nd);
                 if (RES) wa.add(work[u] ? slot[u] : -1, dd, nd, a.acc, 1, lane);
             }
@@ -750,7 +771,7 @@ __device__ __forceinline__ void sweep(const IterArgs& a, int beg, int end, WarpA
                 if (work[u]) primal_load<MODE, CG>(a, pos[u], L[u]);
 #pragma unroll
             for (int u = 0; u < ILP; ++u) {
-                double dd = 0.0, nd = 0.0;
+                float dd = 0.f, nd = 0.f;
                 if (work[u]) primal_finish<RES>(a, pos[u], L[u], dd, nd);
                 if (RES) wa.add(work[u] ? slot[u] : -1, dd, nd, a.acc, 0, lane);
             }
@@ -1148,9 +1169,9 @@ __device__ __forceinline__ void dual_math(const IterArgs& a, const DualLd& L, fl
     q5n = q[5];
 }
 
-// FP64 residual terms of one dual update (as dual_finish computes them).
-__device__ __forceinline__ void dual_res(const DualLd& L, const float4& Po, const float4& Qo, float q5n, double& dd,
-                                         double& nd) {
+// Residual terms of one dual update (as dual_finish computes them).
+__device__ __forceinline__ void dual_res(const DualLd& L, const float4& Po, const float4& Qo, float q5n, float& dd,
+                                         float& nd) {
     const float o[9] = {L.P.x, L.P.y, L.P.z, L.P.w, L.Q.x, L.Q.y, L.Q.z, L.Q.w, L.q5};
     const float w[9] = {Po.x, Po.y, Po.z, Po.w, Qo.x, Qo.y, Qo.z, Qo.w, q5n};
     res_terms<9>(w, o, dd, nd);
@@ -1250,7 +1271,7 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_smem(IterArgs a) {
             int slot = -1;
             if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + o + i) : a.slot0;
             if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
-            double dd = 0.0, nd = 0.0;
+            float dd = 0.f, nd = 0.f;
             if (work) {
                 DualLd L;
                 L.b = s_bar[i]; L.P = s_P[i]; L.Q = s_Q[i]; L.q5 = s_q5[i];
@@ -1274,7 +1295,7 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_smem(IterArgs a) {
             int slot = -1;
             if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + o + i) : a.slot0;
             if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
-            double dd = 0.0, nd = 0.0;
+            float dd = 0.f, nd = 0.f;
             if (work) {
                 PrimalLd L;
                 L.U = s_uv[i]; L.P = s_P[i]; L.Q = s_Q[i]; L.q5 = s_q5[i]; L.D = s_dat[i];
@@ -1407,7 +1428,7 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_dsm(IterArgs a) {
             int slot = -1;
             if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
             if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
-            double dd = 0.0, nd = 0.0;
+            float dd = 0.f, nd = 0.f;
             if (work) {
                 DualLd L;
                 L.b = v.bar[i]; L.P = v.P[i]; L.Q = v.Q[i]; L.q5 = v.q5[i];
@@ -1430,7 +1451,7 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK) k_level_dsm(IterArgs a) {
             int slot = -1;
             if (work) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
             if (STOP && work && MODE == M_STREAM) work = __ldcg(a.done + slot) == 0;
-            double dd = 0.0, nd = 0.0;
+            float dd = 0.f, nd = 0.f;
             if (work) {
                 PrimalLd L;
                 L.U = v.uv[i]; L.P = v.P[i]; L.Q = v.Q[i]; L.q5 = v.q5[i]; L.D = v.dat[i];
@@ -1509,7 +1530,7 @@ __global__ void __launch_bounds__(FT) k_fused(IterArgs a, FuseArgs f) {
         if (own) slot = (MODE == M_STREAM) ? __ldg(a.lid + p) : a.slot0;
         if (STOP && own && MODE == M_STREAM) own = __ldg(a.done + slot) == 0;
         // dual: the tile's own cubes
-        double dd = 0.0, nd = 0.0;
+        float dd = 0.f, nd = 0.f;
         if (own) {
             DualLd L;
             fused_dual_load<MODE>(a, f, p, L);
@@ -1710,7 +1731,7 @@ __global__ void __launch_bounds__(FT) k_fused_tma(IterArgs a, FuseArgs f) {
             slice_bytes(f.slot + (size_t)k * a.npos + t0, 4, cnt, osl[k]);
         }
         slice_bytes(a.dat + t0, 8, cnt, odat);
-        double dd = 0.0, nd = 0.0;
+        float dd = 0.f, nd = 0.f;
         if (own) {
             const int x = threadIdx.x;
             DualLd L;
@@ -1916,7 +1937,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK, 5) k_wave(IterArgs a, WaveArgs w) 
                 bool wk;
                 int sl;
                 const int p = wave_cube<MODE, STOP>(a, w, t, u, wk, sl);
-                double dd = 0.0, nd = 0.0;
+                float dd = 0.f, nd = 0.f;
                 if (wk) dual_cube<MODE, RES, CG>(a, p, dd, nd);
                 if (RES) wd.add(wk ? sl : -1, dd, nd, a.acc, 1, lane);
             }
@@ -1945,7 +1966,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK, 5) k_wave(IterArgs a, WaveArgs w) 
                 bool wk;
                 int sl;
                 const int p = wave_cube<MODE, STOP>(a, w, t, u, wk, sl);
-                double dd = 0.0, nd = 0.0;
+                float dd = 0.f, nd = 0.f;
                 if (wk) primal_cube<MODE, RES, CG>(a, p, dd, nd);
                 if (RES) wp.add(wk ? sl : -1, dd, nd, a.acc, 0, lane);
             }
