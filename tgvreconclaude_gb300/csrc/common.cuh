@@ -184,6 +184,7 @@ struct tgvg_ctx {
     int cluster_max[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};  // usable cluster size per mode / stop (-1 unknown)
     int iter_occ[3][2][2] = {};        // blocks/SM of the sweep kernels [mode][register-capped][dual, primal]
     int iter_occ_ilp2[3][2] = {};      // blocks/SM of the two-cubes-per-thread sweep kernels [mode][dual, primal]
+    int iter_occ_res[3][2] = {};       // blocks/SM of the residual-summing sweep kernels [mode][dual, primal]
     int fused_occ[3][2] = {};          // blocks/SM of the fused iteration kernels per mode [plain, TMA-staged]
     const void* fuse_cur = nullptr;    // the fused-schedule tables of the level being run (tgv.cu), or null
     const void* wave_cur = nullptr;    // the wavefront-schedule tables of the level being run (tgv.cu), or null

@@ -2019,11 +2019,18 @@ static void launch_pdl(void (*k)(KArgs...), unsigned grid, unsigned block, cudaS
     launch_pdl_smem(k, grid, block, 0, s, args...);
 }
 
+// The residual-summing variants (one iteration in check_every) keep the old
+// and new state of a cube and the slot's sums live: at the 40-register bound of
+// six blocks per SM they spilled 60-124 bytes per thread, and a checking
+// iteration cost about twice a plain one.  They run at four blocks per SM.
+constexpr int RES_MINB = 4;
 template <int MODE>
 static void launch_iter(tgvg_ctx* ctx, IterArgs a, bool res, bool stop, bool dual, bool lean, bool ilp2) {
     // One full wave: as many blocks as fit on the GPU at once (occupancy of the
     // variant), each owning an equal contiguous chunk of the unit.
-    const int occ = ilp2 ? ctx->iter_occ_ilp2[MODE][dual ? 0 : 1] : ctx->iter_occ[MODE][lean ? 1 : 0][dual ? 0 : 1];
+    const int occ = ilp2  ? ctx->iter_occ_ilp2[MODE][dual ? 0 : 1]
+                    : res ? ctx->iter_occ_res[MODE][dual ? 0 : 1]
+                          : ctx->iter_occ[MODE][lean ? 1 : 0][dual ? 0 : 1];
     const int want = std::max(1, std::min((a.n + ITER_BLOCK - 1) / ITER_BLOCK, occ * ctx->sm_count));
     a.chunk = ((a.n + want - 1) / want + 31) / 32 * 32;
     const unsigned grid = (unsigned)((a.n + a.chunk - 1) / a.chunk);
@@ -2033,8 +2040,8 @@ static void launch_iter(tgvg_ctx* ctx, IterArgs a, bool res, bool stop, bool dua
     else if (ilp2 && res) k = K<MODE, true, false, 4, 2>;   \
     else if (ilp2 && stop) k = K<MODE, false, true, 4, 2>;  \
     else if (ilp2) k = K<MODE, false, false, 4, 2>;         \
-    else if (res && stop) k = K<MODE, true, true, 6>;       \
-    else if (res) k = K<MODE, true, false, 6>;              \
+    else if (res && stop) k = K<MODE, true, true, RES_MINB>; \
+    else if (res) k = K<MODE, true, false, RES_MINB>;        \
     else if (stop) k = K<MODE, false, true, 6>;             \
     else if (lean) k = K<MODE, false, false, 8>;            \
     else k = K<MODE, false, false, 6>;
@@ -2056,6 +2063,11 @@ static int iter_occupancy(tgvg_ctx* ctx) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v[2], k_dual<MODE, false, false, 8>, ITER_BLOCK, 0);
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v[3], k_primal<MODE, false, false, 8>, ITER_BLOCK, 0);
+    int r[2] = {0, 0};
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r[0], k_dual<MODE, true, true, RES_MINB>, ITER_BLOCK, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r[1], k_primal<MODE, true, true, RES_MINB>, ITER_BLOCK, 0);
     int w[2] = {0, 0};
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w[0], k_dual<MODE, false, false, 4, 2>, ITER_BLOCK, 0);
@@ -2063,6 +2075,8 @@ static int iter_occupancy(tgvg_ctx* ctx) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w[1], k_primal<MODE, false, false, 4, 2>, ITER_BLOCK, 0);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy query");
     o[0] = std::max(1, v[0]); o[1] = std::max(1, v[1]); o[2] = std::max(1, v[2]); o[3] = std::max(1, v[3]);
+    ctx->iter_occ_res[MODE][0] = std::max(1, r[0]);
+    ctx->iter_occ_res[MODE][1] = std::max(1, r[1]);
     ctx->iter_occ_ilp2[MODE][0] = std::max(1, w[0]);
     ctx->iter_occ_ilp2[MODE][1] = std::max(1, w[1]);
     return TGVG_OK;
