@@ -384,9 +384,9 @@ __device__ __forceinline__ void two_sum(float& hi, float& lo, float x) {
 // Accumulate two sums of per-cube FP32 terms over a warp's cubes of one slot,
 // and add them to acc[slot*4+k0..] in FP64 with one atomic per warp per slot
 // run (positions are sorted by leaf).  Within the warp the sums are two-term
-// floats: GB300's FP64 rate is a small fraction of its FP32 rate, and FP64
-// adds per cube made a checking iteration cost about twice a plain one on the
-// largest levels.  Only lane 0 converts to FP64, for the atomic.
+// floats, so the per-cube path has no FP64 arithmetic (GB300's FP64 rate is a
+// small fraction of its FP32 rate); only lane 0 converts to FP64, for the
+// atomic.
 struct WarpAcc {
     float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f;
     int cur = -1;
@@ -495,8 +495,8 @@ __device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const floa
 // rounding in component order (the oracle sums them the same way); the sums
 // over cubes are two-term floats within a warp and FP64 across warps (WarpAcc).
 // GB300's FP64 rate is a small fraction of its FP32 rate: with the per-cube
-// terms in FP64 a checking iteration cost 3.6 times a plain one on the largest
-// levels.
+// terms in FP64 a checking iteration cost about five times a plain one on the
+// largest levels.
 template <int K>
 __device__ __forceinline__ void res_terms(const float* w, const float* o, float& dd, float& nd) {
     float t = fsub(w[0], o[0]);
