@@ -352,6 +352,43 @@ def test_tgv_stopping_rule(oracle_lib):
         assert_state_equal(out, ref, f"stop {mode}")
 
 
+@pytest.mark.parametrize("mode", ["inmem", "stream"])
+def test_coarse_neighbour_ghosts(oracle_lib, mode):
+    """Levels of at least 16,384 cubes copy the p/q values their -x/-y/-z
+    coarser neighbours give into a compact table at the level's start, and the
+    per-launch sweep schedules gather from it.  Every schedule that reads it
+    (per-sweep launches in chunk and band order, two cubes per thread, L2
+    prefetch, the L1 wavefront, the single block), fixed count and
+    tolerance-stopped, must give the oracle's state bit for bit."""
+    ctx = api.context()
+    rng = np.random.default_rng(77)
+    cubes = S.random_octree(rng, dmin=3, dmax=8, target=150000, shape="sphere")
+    depth = cubes["depth"]
+    assert np.bincount(depth).max() >= 16384
+    hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.0)
+    leaves = S.split_leaves(len(cubes), 4, rng, cubes, aligned=True)
+    nb = oracle_lib.neighbour_table(cubes)
+    big = np.bincount(depth).argmax()
+    fine = np.where(depth == big)[0]
+    minus = nb[fine][:, [1, 3, 5]]
+    coarse = (minus >= 0) & (depth[np.maximum(minus, 0)] < big)
+    assert coarse.mean() > 0.05  # the largest level has coarser neighbours to copy
+    fixed, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 30, nthreads=8)
+    stop, rst = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 200, tol=1e-3, check_every=10,
+                                     nthreads=8)
+    try:
+        for cfg in (0, 8, 14, 15, 16, 21, 22):
+            ctx.set_schedule(mode, -1, cfg)
+            out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=30))
+            assert_state_equal(out, fixed, f"ghosts schedule {cfg} {mode}")
+            out, st = api.tgv_solve(cubes, hists, leaves, mode,
+                                    api.TGVParams(alpha0=2.0, alpha1=1.0, iters=200, tol=1e-3, check_every=10))
+            assert_state_equal(out, stop, f"ghosts schedule {cfg} {mode} stopping")
+            assert st["iters_run"] == [r["iters_run"] for r in rst]
+    finally:
+        ctx.set_schedule(mode, -1, -1)
+
+
 def test_stream_leaves_stop_apart_within_a_level(oracle_lib):
     """Streaming semantics, per-launch schedules: within one level some leaves
     meet the tolerance while another runs to the cap (its cubes have no votes, so

@@ -163,6 +163,8 @@ enum BufId {
     // ordered-wavefront schedule tables
     B_W_KEYS, B_W_SKEYS, B_W_KEEP, B_W_POS, B_W_UKEYS, B_W_DEP, B_W_DOFF, B_W_FLAG, B_W_CNT, B_W_TMP, B_W_TMP2,
     B_W_GSTART, B_LVENERGY,
+    // coarser-neighbour ghost tables of the per-launch sweep schedules
+    B_G_PNB, B_G_VAL, B_G_MARK, B_G_IDS, B_G_SUMS,
     B_COUNT
 };
 
@@ -254,4 +256,6 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
 int pyramid_dims(int32_t w, int32_t h, int32_t* dims);
 // Exclusive scan of n ints on the context stream; *total receives the sum (synchronises).
 int scan_exclusive(tgvg_ctx* ctx, const int* d_in, int64_t n, int* d_out, int64_t* total);
+int64_t scan_sums_len(int64_t n);
+int scan_exclusive_async(tgvg_ctx* ctx, const int* d_in, int64_t n, int* d_out, int* sums);
 }  // namespace tgvg

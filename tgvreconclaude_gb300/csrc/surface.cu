@@ -118,6 +118,22 @@ __global__ void k_scan_apply(const int* __restrict__ in, int64_t n, const int* _
     }
 }
 
+// out[i] = sum of in[0..i) for i < n, enqueued only (no host synchronisation,
+// so it can be captured into a CUDA graph); sums holds scan_sums_len(n) ints.
+int64_t scan_sums_len(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+int scan_exclusive_async(tgvg_ctx* ctx, const int* d_in, int64_t n, int* d_out, int* sums) {
+    if (n <= 0) return TGVG_OK;
+    const int64_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nt > (int64_t(1) << 30)) return ctx->fail(TGVG_ERR_LIMIT, "scan too long");
+    k_scan_tiles<<<(unsigned)nt, SCAN_THREADS, 0, ctx->stream>>>(d_in, n, sums);
+    TGVG_LAUNCHED(ctx);
+    k_scan_sums<<<1, 1024, 0, ctx->stream>>>(sums, (int)nt);
+    TGVG_LAUNCHED(ctx);
+    k_scan_apply<<<(unsigned)nt, SCAN_THREADS, 0, ctx->stream>>>(d_in, n, sums, d_out);
+    TGVG_LAUNCHED(ctx);
+    return TGVG_OK;
+}
+
 // out[i] = sum of in[0..i) for i < n; returns the total through *total (host).
 int scan_exclusive(tgvg_ctx* ctx, const int* d_in, int64_t n, int* d_out, int64_t* total) {
     *total = 0;

@@ -368,6 +368,11 @@ struct IterArgs {
     int band;             // per-launch schedules: warps stride over the whole unit (grid-stride band)
     int lend;             // end of the level's positions; cubes at lend and beyond are deeper
     int gcap;             // single-block shared-memory schedule: room for staged out-of-unit values
+    // per-launch sweep schedules (in-memory and streaming semantics): the unit's
+    // -x/-y/-z neighbour table [3][n] with coarser neighbours replaced by
+    // -2 - entry of gh, the compact copies of their gathered p/q values (or null)
+    const int* pnb;
+    const float4* gh;
 };
 
 // Error-free addition (Knuth's TwoSum, TAOCP vol. 2, 4.2.2): hi + x = s + e
@@ -586,9 +591,12 @@ __device__ __forceinline__ void primal_load_own(const IterArgs& a, int p, Primal
     L.Q = CG ? ld4<CG>(a.Q4 + p) : ld4L(a.Q4 + p, pol);
     L.q5 = CG ? ld1<CG>(a.Q1 + p) : ld1L(a.Q1 + p, pol);
     L.D = __ldg(a.dat + p);
-    L.j1 = __ldg(a.nb + a.npos + p);
-    L.j3 = __ldg(a.nb + 3 * a.npos + p);
-    L.j5 = __ldg(a.nb + 5 * a.npos + p);
+    const bool g = !CG && a.pnb;
+    const int* jb = g ? a.pnb + (p - a.o) : a.nb + a.npos + p;
+    const int js = g ? a.n : 2 * a.npos;
+    L.j1 = __ldg(jb);
+    L.j3 = __ldg(jb + js);
+    L.j5 = __ldg(jb + 2 * js);
 }
 
 // ... and the p/q of its -x/-y/-z neighbours.  A neighbour found by code can be
@@ -607,6 +615,9 @@ __device__ __forceinline__ void primal_load_gather(const IterArgs& a, int p, Pri
         const float4 a4 = CG ? ld4<CG>(a.P4 + j) : ld4L(a.P4 + j, pol);
         const float4 b4 = CG ? ld4<CG>(a.Q4 + j) : ld4L(a.Q4 + j, pol);
         L.gp10 = a4.x; L.gq10 = a4.w; L.gq13 = b4.z; L.gq14 = b4.w;
+    } else if (!CG && j1 <= -2) {
+        const float4 g = __ldg(a.gh + (-2 - j1));
+        L.gp10 = g.x; L.gq10 = g.y; L.gq13 = g.z; L.gq14 = g.w;
     }
     if (j3 >= 0 && !(MODE == M_STREAM && (j3 & BORDER)) && (j3 & POS_MASK) < a.lend) {
         const int j = j3 & POS_MASK;
@@ -614,6 +625,9 @@ __device__ __forceinline__ void primal_load_gather(const IterArgs& a, int p, Pri
         const float4 a4 = CG ? ld4<CG>(a.P4 + j) : ld4L(a.P4 + j, pol);
         const float4 b4 = CG ? ld4<CG>(a.Q4 + j) : ld4L(a.Q4 + j, pol);
         L.gp31 = a4.y; L.gq31 = b4.x; L.gq33 = b4.z; L.gq35 = (CG ? ld1<CG>(a.Q1 + j) : ld1L(a.Q1 + j, pol));
+    } else if (!CG && j3 <= -2) {
+        const float4 g = __ldg(a.gh + (-2 - j3));
+        L.gp31 = g.x; L.gq31 = g.y; L.gq33 = g.z; L.gq35 = g.w;
     }
     if (j5 >= 0 && !(MODE == M_STREAM && (j5 & BORDER)) && (j5 & POS_MASK) < a.lend) {
         const int j = j5 & POS_MASK;
@@ -621,6 +635,9 @@ __device__ __forceinline__ void primal_load_gather(const IterArgs& a, int p, Pri
         const float4 a4 = CG ? ld4<CG>(a.P4 + j) : ld4L(a.P4 + j, pol);
         const float4 b4 = CG ? ld4<CG>(a.Q4 + j) : ld4L(a.Q4 + j, pol);
         L.gp52 = a4.z; L.gq52 = b4.y; L.gq54 = b4.w; L.gq55 = (CG ? ld1<CG>(a.Q1 + j) : ld1L(a.Q1 + j, pol));
+    } else if (!CG && j5 <= -2) {
+        const float4 g = __ldg(a.gh + (-2 - j5));
+        L.gp52 = g.x; L.gq52 = g.y; L.gq54 = g.z; L.gq55 = g.w;
     }
 }
 
@@ -704,7 +721,9 @@ __device__ __forceinline__ void prefetch_group(const IterArgs& a, int q0, int en
         else if (lane < 12) line = in4 ? a.Q4 + q0 + 8 * k4 : nullptr;
         else if (lane == 12) line = a.Q1 + q0;
         else if (lane < 15) line = q0 + 16 * (lane - 13) < end ? a.dat + q0 + 16 * (lane - 13) : nullptr;
-        else if (lane < 18) line = a.nb + (size_t)(2 * (lane - 15) + 1) * a.npos + q0;
+        else if (lane < 18)
+            line = a.pnb ? a.pnb + (size_t)(lane - 15) * a.n + (q0 - a.o)
+                         : a.nb + (size_t)(2 * (lane - 15) + 1) * a.npos + q0;
     }
     if (line && q0 < end) asm volatile("prefetch.global.L2 [%0];" ::"l"(line));
 }
@@ -1010,6 +1029,86 @@ __global__ void k_energy(int o, int cnt, int npos, const int* __restrict__ nb, c
     }
     for (int w = 16; w > 0; w >>= 1) e += __shfl_xor_sync(0xffffffffu, e, w);
     if ((threadIdx.x & 31) == 0 && e != 0.0) atomicAdd(out, e);
+}
+
+// ---- coarser-neighbour ghosts (per-launch sweep schedules) -------------------
+// A -x/-y/-z neighbour on a coarser level (a position before the level) does
+// not change while the level runs.  On the finest level of a ray-cast octree
+// about 40 % of those faces have one, and each gather of it read two or three
+// 32-byte sectors of P4/Q4/Q1 for the coarse cube's four values, in every
+// iteration.  At the level's start the four values of each referenced (coarse
+// cube, face) pair are copied to one float4 of a compact array, in the order
+// of first reference, and the level's own -face table points to it
+// (-2 - entry).  Cubes that share a coarse neighbour across a face are
+// siblings (same parent, so at most 8 consecutive positions): a pair is stored
+// once per sibling run.  The copied values are the ones the gather would read,
+// so results are bit-identical.
+static constexpr int GHOST_MIN = 16384;  // smaller levels keep the plain gathers
+
+template <int MODE>
+__device__ __forceinline__ bool coarse_face(int raw, int o) {
+    return raw >= 0 && !(MODE == M_STREAM && (raw & BORDER)) && (raw & POS_MASK) < o;
+}
+
+// The first position of p's sibling run whose neighbour across the face is the
+// same (raw) value; p when none before it.  Positions without a parent form no run.
+__device__ __forceinline__ int ghost_first(const int* __restrict__ nbf, const int* __restrict__ par, int o, int p,
+                                           int raw) {
+    const int pp = par[p];
+    int q0 = p;
+    if (pp < 0) return q0;
+    for (int q = p - 1; q >= max(o, p - 7); --q) {
+        if (par[q] != pp) break;
+        if (nbf[q] == raw) q0 = q;
+    }
+    return q0;
+}
+
+// mark[f*cnt + i] = 1 where position o + i starts a new ghost entry for face
+// 2f+1 (f = 0, 1, 2: -x, -y, -z).
+template <int MODE>
+__global__ void k_ghost_mark(int o, int cnt, int npos, const int* __restrict__ nb, const int* __restrict__ par,
+                             int* __restrict__ mark) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * (int64_t)cnt) return;
+    const int f = int(t / cnt), i = int(t - (int64_t)f * cnt), p = o + i;
+    const int* nbf = nb + (size_t)(2 * f + 1) * npos;
+    const int raw = nbf[p];
+    mark[t] = coarse_face<MODE>(raw, o) && ghost_first(nbf, par, o, p, raw) == p;
+}
+
+// The level's -face table (pnb[f*cnt + i]) and the ghost entries; ids is the
+// exclusive scan of mark.  A face whose run start did not open an entry (a run
+// longer than a sibling group, which a 2:1-balanced octree does not have) keeps
+// its plain neighbour index.
+template <int MODE>
+__global__ void k_ghost_fill(int o, int cnt, int npos, const int* __restrict__ nb, const int* __restrict__ par,
+                             const int* __restrict__ mark, const int* __restrict__ ids, const float4* __restrict__ P4,
+                             const float4* __restrict__ Q4, const float* __restrict__ Q1, int* __restrict__ pnb,
+                             float4* __restrict__ gh) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * (int64_t)cnt) return;
+    const int f = int(t / cnt), i = int(t - (int64_t)f * cnt), p = o + i;
+    const int* nbf = nb + (size_t)(2 * f + 1) * npos;
+    const int raw = nbf[p];
+    if (!coarse_face<MODE>(raw, o)) {
+        pnb[t] = raw;
+        return;
+    }
+    const int q = ghost_first(nbf, par, o, p, raw);
+    if (!mark[(int64_t)f * cnt + (q - o)]) {
+        pnb[t] = raw;
+        return;
+    }
+    const int e = ids[(int64_t)f * cnt + (q - o)];
+    pnb[t] = -2 - e;
+    if (q != p) return;
+    const int j = raw & POS_MASK;
+    const float4 A = P4[j], B = Q4[j];
+    // the values each face's gather takes (primal_load_gather)
+    gh[e] = f == 0 ? make_float4(A.x, A.w, B.z, B.w)
+          : f == 1 ? make_float4(A.y, B.x, B.z, Q1[j])
+                   : make_float4(A.z, B.y, B.w, Q1[j]);
 }
 
 // Streaming semantics, tolerance-stopped solve: at each level's start a leaf's
@@ -3146,6 +3245,22 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         }
         levels.push_back(std::move(lvl));
     }
+    // coarser-neighbour ghost tables for levels run by the per-launch sweep
+    // schedules (in-memory and streaming semantics, state on the device)
+    int gmax = 0;
+    if (mode != M_OC && !paged)
+        for (const Level& lvl : levels)
+            if (lvl.cnt >= GHOST_MIN) gmax = std::max(gmax, lvl.cnt);
+    int *g_pnb = nullptr, *g_mark = nullptr, *g_ids = nullptr, *g_sums = nullptr;
+    float4* g_val = nullptr;
+    if (gmax > 0) {
+        g_pnb = (int*)B(B_G_PNB, 12ull * gmax);
+        g_val = (float4*)B(B_G_VAL, 48ull * gmax);
+        g_mark = (int*)B(B_G_MARK, 12ull * gmax);
+        g_ids = (int*)B(B_G_IDS, 12ull * gmax);
+        g_sums = (int*)B(B_G_SUMS, 4ull * scan_sums_len(3ll * gmax));
+        if (!g_pnb || !g_val || !g_mark || !g_ids || !g_sums) return TGVG_ERR_NOMEM;
+    }
     const int nlv = std::min<int>((int)levels.size(), TGVG_MAX_LEVELS);
     double* lv_res = nullptr;
     int* lv_it = nullptr;
@@ -3202,6 +3317,24 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                 k_copy4<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, bar, snap);
                 TGVG_LAUNCHED(ctx);
             }
+            const bool ghosts = gmax > 0 && cnt >= GHOST_MIN;
+            if (ghosts) {
+                const unsigned gb = (unsigned)((3ll * cnt + 255) / 256);
+                if (mode == M_STREAM)
+                    k_ghost_mark<M_STREAM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark);
+                else
+                    k_ghost_mark<M_INMEM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark);
+                TGVG_LAUNCHED(ctx);
+                const int rc = scan_exclusive_async(ctx, g_mark, 3ll * cnt, g_ids, g_sums);
+                if (rc) return rc;
+                if (mode == M_STREAM)
+                    k_ghost_fill<M_STREAM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark, g_ids, P4, Q4,
+                                                                        Q1, g_pnb, g_val);
+                else
+                    k_ghost_fill<M_INMEM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark, g_ids, P4, Q4,
+                                                                       Q1, g_pnb, g_val);
+                TGVG_LAUNCHED(ctx);
+            }
             // Every slot's iteration count starts at the full count: the fused
             // schedules' settle step reads it in fixed-count solves too, so a
             // count left by an earlier tolerance-stopped solve must not survive.
@@ -3233,6 +3366,8 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                 a.bar_gen = reinterpret_cast<unsigned*>(flags + 5);
                 a.err = flags + 6;
                 a.iters_run = iters_run; a.resid = resid;
+                a.pnb = ghosts ? g_pnb : nullptr;
+                a.gh = ghosts ? g_val : nullptr;
                 set_fuse(Ld);
                 const int rc = run_unit(ctx, mode, a, iters, stop, Ld == t_level, u.cfg, &used_cfg);
                 if (rc) { nvtxRangePop(); return rc; }
@@ -3279,7 +3414,8 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         const void* ptrs[] = {nb, par, uv, bar, P4, Q4, Q1, dat, snap, lid, acc, flags, resid, lv_res,
                               fused_ok ? fz0.barB : nullptr, fused_ok ? fz0.P4B : nullptr,
                               fused_ok ? fz0.Q4B : nullptr, fused_ok ? fz0.Q1B : nullptr,
-                              fused_ok ? fz0.slot : nullptr, fused_ok ? fz0.halo : nullptr};
+                              fused_ok ? fz0.slot : nullptr, fused_ok ? fz0.halo : nullptr,
+                              g_pnb, g_val, g_mark, g_ids, g_sums};
         for (const void* q : ptrs) key.push_back((uint64_t)(uintptr_t)q);
         for (const Level& lvl : levels) {
             key.push_back(((uint64_t)lvl.d << 32) | (uint32_t)lvl.o);
