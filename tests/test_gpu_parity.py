@@ -354,10 +354,9 @@ def test_tgv_stopping_rule(oracle_lib):
 
 @pytest.mark.parametrize("mode", ["inmem", "stream"])
 def test_coarse_neighbour_ghosts(oracle_lib, mode):
-    """Levels of at least 16,384 cubes copy, at the level's start, the p/q
-    values their -x/-y/-z coarser neighbours give and the bars their +x/+y/+z
-    coarser or deeper neighbours give into compact tables, and the per-launch
-    sweep schedules gather from those.  Every schedule that reads them
+    """Levels of at least 16,384 cubes copy the p/q values their -x/-y/-z
+    coarser neighbours give into a compact table at the level's start, and the
+    per-launch sweep schedules gather from it.  Every schedule that reads it
     (per-sweep launches in chunk and band order, two cubes per thread, L2
     prefetch, the L1 wavefront, the single block), fixed count and
     tolerance-stopped, must give the oracle's state bit for bit."""

@@ -373,10 +373,6 @@ struct IterArgs {
     // -2 - entry of gh, the compact copies of their gathered p/q values (or null)
     const int* pnb;
     const float4* gh;
-    // the same for the dual sweep's +x/+y/+z faces: neighbours on other levels
-    // (coarser or deeper) redirected to dgh, copies of their bars (or null)
-    const int* dnb;
-    const float4* dgh;
 };
 
 // Error-free addition (Knuth's TwoSum, TAOCP vol. 2, 4.2.2): hi + x = s + e
@@ -493,8 +489,8 @@ template <bool CG> __device__ __forceinline__ float ld1(const float* p) { return
 
 template <int MODE, bool CG>
 __device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const float4* __restrict__ bar,
-                                            const float4* __restrict__ snap, const float4* __restrict__ gh) {
-    if (j < 0) return (!CG && j <= -2) ? __ldg(gh + (-2 - j)) : own;
+                                            const float4* __restrict__ snap) {
+    if (j < 0) return own;
     if (MODE != M_INMEM && (j & BORDER)) return snap[j & POS_MASK];
     return ld4<CG>(bar + j);
 }
@@ -530,16 +526,13 @@ struct DualLd { float4 b, B0, B2, B4, P, Q; float q5; };
 template <int MODE, bool CG>
 __device__ __forceinline__ void dual_load(const IterArgs& a, int p, DualLd& L) {
     L.b = ld4<CG>(a.bar + p);
-    const bool g = !CG && a.dnb;
-    const int* jb = g ? a.dnb + (p - a.o) : a.nb + p;
-    const int js = g ? a.n : 2 * a.npos;
-    const int j0 = __ldg(jb), j2 = __ldg(jb + js), j4 = __ldg(jb + 2 * js);
+    const int j0 = __ldg(a.nb + p), j2 = __ldg(a.nb + 2 * a.npos + p), j4 = __ldg(a.nb + 4 * a.npos + p);
     L.P = ld4<CG>(a.P4 + p);
     L.Q = ld4<CG>(a.Q4 + p);
     L.q5 = ld1<CG>(a.Q1 + p);
-    L.B0 = fetch_bar<MODE, CG>(j0, L.b, a.bar, a.snap, a.dgh);
-    L.B2 = fetch_bar<MODE, CG>(j2, L.b, a.bar, a.snap, a.dgh);
-    L.B4 = fetch_bar<MODE, CG>(j4, L.b, a.bar, a.snap, a.dgh);
+    L.B0 = fetch_bar<MODE, CG>(j0, L.b, a.bar, a.snap);
+    L.B2 = fetch_bar<MODE, CG>(j2, L.b, a.bar, a.snap);
+    L.B4 = fetch_bar<MODE, CG>(j4, L.b, a.bar, a.snap);
 }
 
 template <bool RES>
@@ -721,8 +714,7 @@ __device__ __forceinline__ void prefetch_group(const IterArgs& a, int q0, int en
         else if (lane < 8) line = in4 ? a.P4 + q0 + 8 * k4 : nullptr;
         else if (lane < 12) line = in4 ? a.Q4 + q0 + 8 * k4 : nullptr;
         else if (lane == 12) line = a.Q1 + q0;
-        else if (lane < 16)
-            line = a.dnb ? a.dnb + (size_t)(lane - 13) * a.n + (q0 - a.o) : a.nb + (size_t)(2 * (lane - 13)) * a.npos + q0;
+        else if (lane < 16) line = a.nb + (size_t)(2 * (lane - 13)) * a.npos + q0;
     } else {
         if (lane < 4) line = in4 ? a.uv + q0 + 8 * k4 : nullptr;
         else if (lane < 8) line = in4 ? a.P4 + q0 + 8 * k4 : nullptr;
@@ -1039,31 +1031,23 @@ __global__ void k_energy(int o, int cnt, int npos, const int* __restrict__ nb, c
     if ((threadIdx.x & 31) == 0 && e != 0.0) atomicAdd(out, e);
 }
 
-// ---- neighbour ghosts (per-launch sweep schedules) ---------------------------
-// A neighbour on another level does not change while a level runs: a coarser
-// one has finished, a deeper one has not started.  On the finest level of a
-// ray-cast octree about 40 % of the -x/-y/-z faces have a coarser neighbour,
-// and each gather of it read two or three 32-byte sectors of P4/Q4/Q1 for the
-// coarse cube's four values, in every iteration; the dual's +x/+y/+z faces
-// read a coarser or deeper cube's bar the same way.  At the level's start the
-// values each face takes from such a neighbour are copied to one float4 of a
-// compact array, one entry per referenced (neighbour, face), in the order of
-// first reference, and the level's own face table points to it (-2 - entry).
-// Cubes that share a neighbour on another level across a face are siblings
-// (it is their parent's neighbour), so at most 8 consecutive positions: the
-// first of them owns the entry.  The copies are the values the gathers would
-// read, so results are bit-identical.
+// ---- coarser-neighbour ghosts (per-launch sweep schedules) -------------------
+// A -x/-y/-z neighbour on a coarser level (a position before the level) does
+// not change while the level runs.  On the finest level of a ray-cast octree
+// about 40 % of those faces have one, and each gather of it read two or three
+// 32-byte sectors of P4/Q4/Q1 for the coarse cube's four values, in every
+// iteration.  At the level's start the four values of each referenced (coarse
+// cube, face) pair are copied to one float4 of a compact array, in the order
+// of first reference, and the level's own -face table points to it
+// (-2 - entry).  Cubes that share a coarse neighbour across a face are
+// siblings (same parent, so at most 8 consecutive positions): a pair is stored
+// once per sibling run.  The copied values are the ones the gather would read,
+// so results are bit-identical.
 static constexpr int GHOST_MIN = 16384;  // smaller levels keep the plain gathers
 
-// PRIMAL: the primal sweep's -x/-y/-z faces, which read coarser neighbours'
-// p/q (a deeper neighbour's p/q are zero and are not loaded at all).  Else
-// the dual sweep's +x/+y/+z faces, which read a coarser or deeper neighbour's
-// bar.  A frozen border neighbour (streaming) reads the snapshot instead.
-template <int MODE, bool PRIMAL>
-__device__ __forceinline__ bool ghost_face(int raw, int o, int lend) {
-    if (raw < 0 || (MODE == M_STREAM && (raw & BORDER))) return false;
-    const int j = raw & POS_MASK;
-    return PRIMAL ? j < o : (j < o || j >= lend);
+template <int MODE>
+__device__ __forceinline__ bool coarse_face(int raw, int o) {
+    return raw >= 0 && !(MODE == M_STREAM && (raw & BORDER)) && (raw & POS_MASK) < o;
 }
 
 // The first position of p's sibling run whose neighbour across the face is the
@@ -1080,77 +1064,51 @@ __device__ __forceinline__ int ghost_first(const int* __restrict__ nbf, const in
     return q0;
 }
 
-// mark[f*cnt + i] = 1 where position o + i opens a new ghost entry for its
-// face f (0, 1, 2 = x, y, z on the sweep's side).
-template <int MODE, bool PRIMAL>
+// mark[f*cnt + i] = 1 where position o + i starts a new ghost entry for face
+// 2f+1 (f = 0, 1, 2: -x, -y, -z).
+template <int MODE>
 __global__ void k_ghost_mark(int o, int cnt, int npos, const int* __restrict__ nb, const int* __restrict__ par,
                              int* __restrict__ mark) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * (int64_t)cnt) return;
     const int f = int(t / cnt), i = int(t - (int64_t)f * cnt), p = o + i;
-    const int* nbf = nb + (size_t)(2 * f + (PRIMAL ? 1 : 0)) * npos;
+    const int* nbf = nb + (size_t)(2 * f + 1) * npos;
     const int raw = nbf[p];
-    mark[t] = ghost_face<MODE, PRIMAL>(raw, o, o + cnt) && ghost_first(nbf, par, o, p, raw) == p;
+    mark[t] = coarse_face<MODE>(raw, o) && ghost_first(nbf, par, o, p, raw) == p;
 }
 
-// The level's face table (fnb[f*cnt + i]) and the ghost entries; ids is the
+// The level's -face table (pnb[f*cnt + i]) and the ghost entries; ids is the
 // exclusive scan of mark.  A face whose run start did not open an entry (a run
-// longer than a sibling group, which the octree does not have) keeps its
-// plain neighbour index.
-template <int MODE, bool PRIMAL>
+// longer than a sibling group, which a 2:1-balanced octree does not have) keeps
+// its plain neighbour index.
+template <int MODE>
 __global__ void k_ghost_fill(int o, int cnt, int npos, const int* __restrict__ nb, const int* __restrict__ par,
                              const int* __restrict__ mark, const int* __restrict__ ids, const float4* __restrict__ P4,
-                             const float4* __restrict__ Q4, const float* __restrict__ Q1,
-                             const float4* __restrict__ bar, int* __restrict__ fnb, float4* __restrict__ gh) {
+                             const float4* __restrict__ Q4, const float* __restrict__ Q1, int* __restrict__ pnb,
+                             float4* __restrict__ gh) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * (int64_t)cnt) return;
     const int f = int(t / cnt), i = int(t - (int64_t)f * cnt), p = o + i;
-    const int* nbf = nb + (size_t)(2 * f + (PRIMAL ? 1 : 0)) * npos;
+    const int* nbf = nb + (size_t)(2 * f + 1) * npos;
     const int raw = nbf[p];
-    if (!ghost_face<MODE, PRIMAL>(raw, o, o + cnt)) {
-        fnb[t] = raw;
+    if (!coarse_face<MODE>(raw, o)) {
+        pnb[t] = raw;
         return;
     }
     const int q = ghost_first(nbf, par, o, p, raw);
     if (!mark[(int64_t)f * cnt + (q - o)]) {
-        fnb[t] = raw;
+        pnb[t] = raw;
         return;
     }
     const int e = ids[(int64_t)f * cnt + (q - o)];
-    fnb[t] = -2 - e;
+    pnb[t] = -2 - e;
     if (q != p) return;
     const int j = raw & POS_MASK;
-    if (!PRIMAL) {
-        gh[e] = bar[j];
-        return;
-    }
     const float4 A = P4[j], B = Q4[j];
     // the values each face's gather takes (primal_load_gather)
     gh[e] = f == 0 ? make_float4(A.x, A.w, B.z, B.w)
           : f == 1 ? make_float4(A.y, B.x, B.z, Q1[j])
                    : make_float4(A.z, B.y, B.w, Q1[j]);
-}
-
-// Both ghost tables of a level (mark and ids are scratch, reused in turn).
-template <int MODE>
-static int build_ghosts(tgvg_ctx* ctx, int o, int cnt, int npos, const int* nb, const int* par,
-                        const float4* P4, const float4* Q4, const float* Q1, const float4* bar, int* mark, int* ids,
-                        int* sums, int* pnb, float4* gh, int* dnb, float4* dgh) {
-    const unsigned gb = (unsigned)((3ll * cnt + 255) / 256);
-    k_ghost_mark<MODE, true><<<gb, 256, 0, ctx->stream>>>(o, cnt, npos, nb, par, mark);
-    TGVG_LAUNCHED(ctx);
-    int rc = scan_exclusive_async(ctx, mark, 3ll * cnt, ids, sums);
-    if (rc) return rc;
-    k_ghost_fill<MODE, true><<<gb, 256, 0, ctx->stream>>>(o, cnt, npos, nb, par, mark, ids, P4, Q4, Q1, bar, pnb,
-                                                          gh);
-    TGVG_LAUNCHED(ctx);
-    k_ghost_mark<MODE, false><<<gb, 256, 0, ctx->stream>>>(o, cnt, npos, nb, par, mark);
-    TGVG_LAUNCHED(ctx);
-    if ((rc = scan_exclusive_async(ctx, mark, 3ll * cnt, ids, sums))) return rc;
-    k_ghost_fill<MODE, false><<<gb, 256, 0, ctx->stream>>>(o, cnt, npos, nb, par, mark, ids, P4, Q4, Q1, bar, dnb,
-                                                           dgh);
-    TGVG_LAUNCHED(ctx);
-    return TGVG_OK;
 }
 
 // Streaming semantics, tolerance-stopped solve: at each level's start a leaf's
@@ -3293,17 +3251,15 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     if (mode != M_OC && !paged)
         for (const Level& lvl : levels)
             if (lvl.cnt >= GHOST_MIN) gmax = std::max(gmax, lvl.cnt);
-    int *g_pnb = nullptr, *g_dnb = nullptr, *g_mark = nullptr, *g_ids = nullptr, *g_sums = nullptr;
-    float4 *g_val = nullptr, *g_dval = nullptr;
+    int *g_pnb = nullptr, *g_mark = nullptr, *g_ids = nullptr, *g_sums = nullptr;
+    float4* g_val = nullptr;
     if (gmax > 0) {
         g_pnb = (int*)B(B_G_PNB, 12ull * gmax);
         g_val = (float4*)B(B_G_VAL, 48ull * gmax);
-        g_dnb = (int*)B(B_G_DNB, 12ull * gmax);
-        g_dval = (float4*)B(B_G_DVAL, 48ull * gmax);
         g_mark = (int*)B(B_G_MARK, 12ull * gmax);
         g_ids = (int*)B(B_G_IDS, 12ull * gmax);
         g_sums = (int*)B(B_G_SUMS, 4ull * scan_sums_len(3ll * gmax));
-        if (!g_pnb || !g_val || !g_dnb || !g_dval || !g_mark || !g_ids || !g_sums) return TGVG_ERR_NOMEM;
+        if (!g_pnb || !g_val || !g_mark || !g_ids || !g_sums) return TGVG_ERR_NOMEM;
     }
     const int nlv = std::min<int>((int)levels.size(), TGVG_MAX_LEVELS);
     double* lv_res = nullptr;
@@ -3363,12 +3319,21 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
             }
             const bool ghosts = gmax > 0 && cnt >= GHOST_MIN;
             if (ghosts) {
-                const int rc = mode == M_STREAM
-                                   ? build_ghosts<M_STREAM>(ctx, o, cnt, n, nb, par, P4, Q4, Q1, bar, g_mark, g_ids,
-                                                            g_sums, g_pnb, g_val, g_dnb, g_dval)
-                                   : build_ghosts<M_INMEM>(ctx, o, cnt, n, nb, par, P4, Q4, Q1, bar, g_mark, g_ids,
-                                                           g_sums, g_pnb, g_val, g_dnb, g_dval);
+                const unsigned gb = (unsigned)((3ll * cnt + 255) / 256);
+                if (mode == M_STREAM)
+                    k_ghost_mark<M_STREAM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark);
+                else
+                    k_ghost_mark<M_INMEM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark);
+                TGVG_LAUNCHED(ctx);
+                const int rc = scan_exclusive_async(ctx, g_mark, 3ll * cnt, g_ids, g_sums);
                 if (rc) return rc;
+                if (mode == M_STREAM)
+                    k_ghost_fill<M_STREAM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark, g_ids, P4, Q4,
+                                                                        Q1, g_pnb, g_val);
+                else
+                    k_ghost_fill<M_INMEM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark, g_ids, P4, Q4,
+                                                                       Q1, g_pnb, g_val);
+                TGVG_LAUNCHED(ctx);
             }
             // Every slot's iteration count starts at the full count: the fused
             // schedules' settle step reads it in fixed-count solves too, so a
@@ -3403,8 +3368,6 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                 a.iters_run = iters_run; a.resid = resid;
                 a.pnb = ghosts ? g_pnb : nullptr;
                 a.gh = ghosts ? g_val : nullptr;
-                a.dnb = ghosts ? g_dnb : nullptr;
-                a.dgh = ghosts ? g_dval : nullptr;
                 set_fuse(Ld);
                 const int rc = run_unit(ctx, mode, a, iters, stop, Ld == t_level, u.cfg, &used_cfg);
                 if (rc) { nvtxRangePop(); return rc; }
@@ -3452,7 +3415,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                               fused_ok ? fz0.barB : nullptr, fused_ok ? fz0.P4B : nullptr,
                               fused_ok ? fz0.Q4B : nullptr, fused_ok ? fz0.Q1B : nullptr,
                               fused_ok ? fz0.slot : nullptr, fused_ok ? fz0.halo : nullptr,
-                              g_pnb, g_val, g_dnb, g_dval, g_mark, g_ids, g_sums};
+                              g_pnb, g_val, g_mark, g_ids, g_sums};
         for (const void* q : ptrs) key.push_back((uint64_t)(uintptr_t)q);
         for (const Level& lvl : levels) {
             key.push_back(((uint64_t)lvl.d << 32) | (uint32_t)lvl.o);
