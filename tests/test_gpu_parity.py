@@ -359,13 +359,16 @@ def test_coarse_neighbour_ghosts(oracle_lib, mode):
     per-launch sweep schedules gather from it.  Every schedule that reads it
     (per-sweep launches in chunk and band order, two cubes per thread, L2
     prefetch, the L1 wavefront, the single block), fixed count and
-    tolerance-stopped, must give the oracle's state bit for bit."""
+    tolerance-stopped, must give the oracle's state bit for bit.  Some cubes
+    have no votes and some vote totals are above 2^28."""
     ctx = api.context()
     rng = np.random.default_rng(77)
     cubes = S.random_octree(rng, dmin=3, dmax=8, target=150000, shape="sphere")
     depth = cubes["depth"]
     assert np.bincount(depth).max() >= 16384
     hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.0)
+    hists[::97, 2] = 300_000_000  # vote totals above 2^28
+    hists[::89] = 0               # cubes without votes
     leaves = S.split_leaves(len(cubes), 4, rng, cubes, aligned=True)
     nb = oracle_lib.neighbour_table(cubes)
     big = np.bincount(depth).argmax()
