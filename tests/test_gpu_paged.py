@@ -7,7 +7,7 @@ tgv_minimize_streaming (reference src/tgv.cpp:802-1070)."""
 import numpy as np
 import pytest
 
-from tgvreconclaude_gb300 import api, formats as F, scenes as S
+from tgvreconclaude_gb300 import _native as N, api, formats as F, scenes as S
 
 pytestmark = pytest.mark.gpu
 BUDGET = 1 << 20
@@ -76,3 +76,29 @@ def test_paged_streaming_files(tmp_path, oracle_lib, budget):
     api.tgv_minimize_streaming(cp, hp, tp, None, 1.0, tmp_path / "s_paged", prm)
     ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, "stream", 2.0, 1.0, 25, nthreads=8)
     same(F.load_state(tmp_path / "s_paged"), ref, "paged file streaming")
+
+
+def test_histograms_in_batches_under_budget(oracle_lib, budget):
+    """Under the budget, compute_histograms bins the cubes in batches (9,362
+    cubes of 56 bytes each here) against pyramids that stay on the device; the
+    histograms equal the oracle's (reference histogram.cpp:115-163)."""
+    rng = np.random.default_rng(814)
+    scene = S.three_objects_scene(rng)
+    rig = S.sphere_rig(6, 6.0, width=160, height=120, half_fov_deg=28)
+    cams, depths, maps = [], [], []
+    for i, c in enumerate(rig):
+        d = S.render_depth(scene, c, seed=900 + i).numpy()
+        rt_inv = np.linalg.inv(np.asarray(c["rt"], np.float64)).astype(np.float32)
+        cam = N.Camera()
+        cam.rt_inv[:] = [float(v) for v in rt_inv.reshape(16)]
+        cam.fx, cam.fy, cam.cx, cam.cy = c["fx"], c["fy"], c["cx"], c["cy"]
+        cam.width, cam.height, cam.lidar = 160, 120, 0
+        cams.append(cam)
+        depths.append(d)
+        maps.append(dict(depth=d, rt_inv=rt_inv, fx=c["fx"], fy=c["fy"], cx=c["cx"], cy=c["cy"], lidar=False))
+    cubes = S.random_octree(rng, dmin=3, dmax=9, target=80000, shape="sphere", r_root=3.0)
+    origin = (-3.0, -3.0, -3.0)
+    ref = oracle_lib.compute_histograms(cubes, maps, origin, 3.0, nbins=10, nthreads=8)
+    gpu = api.compute_histograms_from_maps(cubes, cams, depths, origin, 3.0, nbins=10)
+    assert ref.sum() > 0 and len(cubes) > 3 * (BUDGET // 2) // 56
+    assert np.array_equal(gpu, ref)

@@ -425,9 +425,18 @@ static int histograms_host(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n,
     if (n == 0) return TGVG_OK;
     std::vector<int64_t> off(ncam + 1, 0);
     for (int c = 0; c < ncam; ++c) off[c + 1] = off[c] + pyramid_size(cams[c].width, cams[c].height);
+    // Under a device budget (tgvg_set_device_budget) the cubes go through in
+    // batches whose cube and histogram buffers take at most half of it; the
+    // pyramids stay on the device.  Cubes are binned independently, so the
+    // batches give the one-pass result.
+    int64_t batch = n;
+    if (ctx->device_budget > 0) {
+        const int64_t per = int64_t(sizeof(tgvg_cube)) + 4ll * nbins;
+        batch = std::min<int64_t>(n, std::max<int64_t>(4096, int64_t(ctx->device_budget / 2) / per));
+    }
     float* d_tex = (float*)ctx->buf(B_H_TEX, sizeof(float) * std::max<int64_t>(1, off[ncam]));
-    tgvg_cube* d_cubes = (tgvg_cube*)ctx->buf(B_H_CUBES, sizeof(tgvg_cube) * n);
-    uint32_t* d_out = (uint32_t*)ctx->buf(B_H_OUT, sizeof(uint32_t) * nbins * n);
+    tgvg_cube* d_cubes = (tgvg_cube*)ctx->buf(B_H_CUBES, sizeof(tgvg_cube) * batch);
+    uint32_t* d_out = (uint32_t*)ctx->buf(B_H_OUT, sizeof(uint32_t) * nbins * batch);
     if (!d_tex || !d_cubes || !d_out) return TGVG_ERR_NOMEM;
     for (int c = 0; c < ncam; ++c) {
         if (!maps[c]) return TGVG_ERR_INVALID;
@@ -436,13 +445,16 @@ static int histograms_host(tgvg_ctx* ctx, const tgvg_cube* cubes, int64_t n,
                                      cudaMemcpyHostToDevice, ctx->stream));
     }
     if (!pyr && ncam > 0 && (rc = build_pyramids_dev(ctx, cams, ncam, d_tex, off.data()))) return rc;
-    TGVG_CK(ctx, cudaMemcpyAsync(d_cubes, cubes, sizeof(tgvg_cube) * n, cudaMemcpyHostToDevice,
-                                 ctx->stream));
-    if ((rc = histograms_dev(ctx, d_cubes, n, cams, ncam, d_tex, off.data(), origin, r_root, nbins,
-                             d_out)))
-        return rc;
-    TGVG_CK(ctx, cudaMemcpyAsync(out, d_out, sizeof(uint32_t) * nbins * n, cudaMemcpyDeviceToHost,
-                                 ctx->stream));
+    for (int64_t s0 = 0; s0 < n; s0 += batch) {
+        const int64_t m = std::min(batch, n - s0);
+        TGVG_CK(ctx, cudaMemcpyAsync(d_cubes, cubes + s0, sizeof(tgvg_cube) * m, cudaMemcpyHostToDevice,
+                                     ctx->stream));
+        if ((rc = histograms_dev(ctx, d_cubes, m, cams, ncam, d_tex, off.data(), origin, r_root, nbins,
+                                 d_out)))
+            return rc;
+        TGVG_CK(ctx, cudaMemcpyAsync(out + s0 * nbins, d_out, sizeof(uint32_t) * nbins * m,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+    }
     TGVG_CK(ctx, cudaStreamSynchronize(ctx->stream));
     return TGVG_OK;
 }
