@@ -266,7 +266,9 @@ int tgvg_compute_histograms_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, int64_t
  * with it: make that first call before any stream capture, and before the
  * caller reserves the device's memory for its own pool.  Work is enqueued on
  * `stream` (a cudaStream_t; null = the legacy default stream) and the call
- * returns without waiting.  All calls share the one array, so calls that may
+ * returns without waiting.  The call copies the camera table from host memory
+ * on `stream`, so it cannot be captured into a CUDA graph.  All calls share the
+ * one array, so calls that may
  * overlap on the GPU (other streams, other host threads) race and must be
  * serialised by the caller.  Output is bit-identical to
  * tgvg_compute_histograms_dev. */
@@ -276,7 +278,8 @@ int tgvg_compute_histograms_noalloc(const tgvg_cube* d_cubes, int64_t n, const t
 
 /* compute_histograms_oc (reference src/histogram.hpp:55-61, histogram.cpp:222-256):
  * cubes from a TGV1 file, leaves from the caller, output written as a TGVH file
- * (8 bins).  The whole cube file is processed in one device pass. */
+ * (8 bins).  The whole cube file is processed in one device pass, or in
+ * batches of cubes under a device budget (tgvg_set_device_budget). */
 int tgvg_compute_histograms_oc(tgvg_ctx* ctx, const char* cube_path, const tgvg_leaf* leaves,
                                int32_t nleaf, const tgvg_camera* cams, int32_t ncam,
                                const float* const* base, const float origin[3], float r_root,

@@ -542,27 +542,18 @@ static constexpr int64_t NOALLOC_CAM_FLOATS = 9216;                   // 256 Dev
 static constexpr int64_t NOALLOC_TEX_FLOATS = int64_t(16) << 20;      // 16 Mi texels = 64 MiB
 static __device__ __align__(256) float g_noalloc_scratch[NOALLOC_CAM_FLOATS + NOALLOC_TEX_FLOATS];
 
-namespace {
-std::mutex g_noalloc_mu;
-float* g_noalloc_addr[128] = {};  // device address of g_noalloc_scratch, per device ordinal
-}  // namespace
-
-// Device address of the scratch array on the current device.  The first call
-// on each device looks it up (cudaGetSymbolAddress, which may load the module);
-// later calls reuse it.
+// Device address of the scratch array in the current context.  It is looked
+// up on every call (the first call on a device may load the module): a cached
+// address would go stale if the context were reset and the module reloaded.
 static int noalloc_scratch(float** out) {
     int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return TGVG_ERR_NODEVICE;
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        float* p = nullptr;
-        if (cudaGetSymbolAddress((void**)&p, g_noalloc_scratch) != cudaSuccess || !p) {
-            cudaGetLastError();
-            return TGVG_ERR_CUDA;
-        }
-        g_noalloc_addr[dev] = p;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return TGVG_ERR_NODEVICE;
+    float* p = nullptr;
+    if (cudaGetSymbolAddress((void**)&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return TGVG_ERR_CUDA;
     }
-    *out = g_noalloc_addr[dev];
+    *out = p;
     return TGVG_OK;
 }
 
