@@ -259,3 +259,46 @@ def test_neighbour_table_on_a_uniform_grid(oracle_lib):
             q = list(p)
             q[f // 2] += 1 if f % 2 == 0 else -1
             assert nb[i, f] == pos.get(tuple(q), -1)
+
+
+def test_coarser_neighbours_are_shared_within_sibling_runs(oracle_lib):
+    """The ghost tables of the primal sweep store one entry per (coarser
+    neighbour, face) and sibling run: a cube looks for an earlier cube with the
+    same neighbour value among the previous 7 positions with the same parent.
+    The cubes of a level that reach one coarser cube across a face are the
+    children of at most two parents: the coarse cube's neighbour, and the coarse
+    cube itself where the octree keeps a cube together with cubes inside it (the
+    reference's parent-code lookup, tgv.cpp:97-109).  So each (neighbour, face)
+    has at most two entries, and the dedup is complete within each run if a run
+    spans at most 8 positions.  Checked on the reference-balanced octrees of the
+    fixtures and on random octrees, in the solver's level-major order."""
+    g = np.load(os.path.join(GOLDEN, "octree_cases.npz"))
+    cases = [g[f"bal_out{k}"] for k in (0, 1, 2, 4)]
+    for seed, shape in ((5, "sphere"), (6, "plane"), (7, "random")):
+        cases.append(S.random_octree(np.random.default_rng(seed), dmin=2, dmax=7, target=40000, shape=shape))
+    for cubes in cases:
+        cubes = cubes[np.argsort(F.cube_keys(cubes), kind="stable")]
+        nb = oracle_lib.neighbour_table(cubes)
+        d = cubes["depth"].astype(np.int64)
+        keys = F.cube_keys(cubes).astype(np.uint64)
+        pos = np.empty(len(cubes), np.int64)
+        pos[np.lexsort((np.arange(len(cubes)), d))] = np.arange(len(cubes))
+        parent = (keys >> (np.uint64(3) * (np.uint64(F.MAX_DEPTH) - (d - 1).astype(np.uint64)))).astype(np.int64)
+        checked = 0
+        for f in (1, 3, 5):
+            j = nb[:, f].astype(np.int64)
+            idx = np.nonzero((j >= 0) & (d[np.maximum(j, 0)] < d))[0]
+            if len(idx) == 0:
+                continue
+            _, run = np.unique(np.stack([j[idx], d[idx], parent[idx]], 1), axis=0, return_inverse=True)
+            run = run.ravel()
+            lo = np.full(run.max() + 1, np.iinfo(np.int64).max)
+            hi = np.full(run.max() + 1, np.iinfo(np.int64).min)
+            np.minimum.at(lo, run, pos[idx])
+            np.maximum.at(hi, run, pos[idx])
+            assert (hi - lo).max() <= 7
+            _, grp = np.unique(np.stack([j[idx], d[idx]], 1), axis=0, return_inverse=True)
+            pairs = np.unique(np.stack([grp.ravel(), run], 1), axis=0)
+            assert np.bincount(pairs[:, 0]).max() <= 2
+            checked += len(idx)
+        assert checked > 500

@@ -1039,10 +1039,12 @@ __global__ void k_energy(int o, int cnt, int npos, const int* __restrict__ nb, c
 // iteration.  At the level's start the four values of each referenced (coarse
 // cube, face) pair are copied to one float4 of a compact array, in the order
 // of first reference, and the level's own -face table points to it
-// (-2 - entry).  Cubes that share a coarse neighbour across a face are
-// siblings (same parent, so at most 8 consecutive positions): a pair is stored
-// once per sibling run.  The copied values are the ones the gather would read,
-// so results are bit-identical.
+// (-2 - entry).  Cubes that share a coarse neighbour across a face are the
+// children of at most two parents (the coarse cube's neighbour, and the coarse
+// cube itself where the octree keeps a cube together with cubes inside it);
+// siblings sit in at most 8 consecutive positions, so a pair is stored once per
+// sibling run, at most twice.  The copied values are the ones the gather would
+// read, so results are bit-identical.
 static constexpr int GHOST_MIN = 16384;  // smaller levels keep the plain gathers
 
 template <int MODE>
