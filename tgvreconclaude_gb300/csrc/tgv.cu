@@ -1046,6 +1046,8 @@ __global__ void k_energy(int o, int cnt, int npos, const int* __restrict__ nb, c
 // sibling run, at most twice.  The copied values are the ones the gather would
 // read, so results are bit-identical.
 static constexpr int GHOST_MIN = 16384;  // smaller levels keep the plain gathers
+// entry numbers are int: at most three per cube of the level
+static constexpr int GHOST_MAX = (int)((((int64_t)1 << 31) - 1) / 3);
 
 template <int MODE>
 __device__ __forceinline__ bool coarse_face(int raw, int o) {
@@ -3252,7 +3254,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     int gmax = 0;
     if (mode != M_OC && !paged)
         for (const Level& lvl : levels)
-            if (lvl.cnt >= GHOST_MIN) gmax = std::max(gmax, lvl.cnt);
+            if (lvl.cnt >= GHOST_MIN && lvl.cnt <= GHOST_MAX) gmax = std::max(gmax, lvl.cnt);
     int *g_pnb = nullptr, *g_mark = nullptr, *g_ids = nullptr, *g_sums = nullptr;
     float4* g_val = nullptr;
     if (gmax > 0) {
@@ -3319,7 +3321,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                 k_copy4<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(n, bar, snap);
                 TGVG_LAUNCHED(ctx);
             }
-            const bool ghosts = gmax > 0 && cnt >= GHOST_MIN;
+            const bool ghosts = gmax > 0 && cnt >= GHOST_MIN && cnt <= GHOST_MAX;
             if (ghosts) {
                 const unsigned gb = (unsigned)((3ll * cnt + 255) / 256);
                 if (mode == M_STREAM)
