@@ -392,6 +392,47 @@ def test_coarse_neighbour_ghosts(oracle_lib, mode):
         ctx.set_schedule(mode, -1, -1)
 
 
+def _refined_slab():
+    """A 512 x 512 slab of depth-9 cubes (z cell 0) under a slab of depth-10
+    cubes filling z cell 1: the depth-9 level (262,144 cubes) has a deeper
+    neighbour across every +z face (the depth-10 octant-0 child shares the
+    code), and the depth-10 level a coarser one across every -z face."""
+    sh9, sh10 = F.MAX_DEPTH - 9, F.MAX_DEPTH - 10
+    g9 = np.arange(512, dtype=np.uint64)
+    X, Y = np.meshgrid(g9, g9, indexing="ij")
+    k9 = F.morton_encode(X.ravel() << np.uint64(sh9), Y.ravel() << np.uint64(sh9), np.zeros(X.size, np.uint64))
+    g10 = np.arange(1024, dtype=np.uint64)
+    X, Y = np.meshgrid(g10, g10, indexing="ij")
+    k10 = np.concatenate([F.morton_encode(X.ravel() << np.uint64(sh10), Y.ravel() << np.uint64(sh10),
+                                          np.full(X.size, z << sh10, np.uint64)) for z in (2, 3)])
+    keys = np.concatenate([k9, k10])
+    depth = np.concatenate([np.full(len(k9), 9, np.int32), np.full(len(k10), 10, np.int32)])
+    o = np.argsort(keys, kind="stable")
+    return F.make_cubes(keys[o], depth[o], np.full(len(keys), 0.01, np.float32))
+
+
+@pytest.mark.parametrize("mode", ["inmem", "stream"])
+def test_dual_ghosts_on_a_refined_slab(oracle_lib, mode):
+    """Levels of at least 262,144 cubes whose next level is at least twice as
+    large also copy the bars of the dual sweep's +x/+y/+z neighbours on other
+    levels into a compact table; per-launch schedules (and the schedules that
+    share their loads) read them.  The state must equal the oracle's."""
+    ctx = api.context()
+    cubes = _refined_slab()
+    rng = np.random.default_rng(17)
+    hists = S.random_histograms(rng, len(cubes), nbins=8, empty_frac=0.05)
+    leaves = S.split_leaves(len(cubes), 3, rng, cubes, aligned=True)
+    ref, _ = oracle_lib.tgv_solve(cubes, hists, leaves, mode, 2.0, 1.0, 12, nthreads=8)
+    try:
+        for cfg in (0, 14, 16, 21):
+            ctx.set_schedule(mode, -1, cfg)
+            out, st = api.tgv_solve(cubes, hists, leaves, mode, api.TGVParams(alpha0=2.0, alpha1=1.0, iters=12))
+            assert st["active"][:2] == [262144, 2097152]
+            assert_state_equal(out, ref, f"dual ghosts schedule {cfg} {mode}")
+    finally:
+        ctx.set_schedule(mode, -1, -1)
+
+
 def test_stream_leaves_stop_apart_within_a_level(oracle_lib):
     """Streaming semantics, per-launch schedules: within one level some leaves
     meet the tolerance while another runs to the cap (its cubes have no votes, so

@@ -164,7 +164,7 @@ enum BufId {
     B_W_KEYS, B_W_SKEYS, B_W_KEEP, B_W_POS, B_W_UKEYS, B_W_DEP, B_W_DOFF, B_W_FLAG, B_W_CNT, B_W_TMP, B_W_TMP2,
     B_W_GSTART, B_LVENERGY,
     // coarser-neighbour ghost tables of the per-launch sweep schedules
-    B_G_PNB, B_G_VAL, B_G_MARK, B_G_IDS, B_G_SUMS,
+    B_G_PNB, B_G_VAL, B_G_MARK, B_G_IDS, B_G_SUMS, B_G_DNB, B_G_DVAL,
     B_COUNT
 };
 

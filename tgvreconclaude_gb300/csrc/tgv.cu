@@ -373,6 +373,11 @@ struct IterArgs {
     // -2 - entry of gh, the compact copies of their gathered p/q values (or null)
     const int* pnb;
     const float4* gh;
+    // the same for the dual sweep's +x/+y/+z faces on levels with many deeper
+    // neighbours: neighbours on other levels redirected to dgh, copies of their
+    // bars (or null)
+    const int* dnb;
+    const float4* dgh;
 };
 
 // Error-free addition (Knuth's TwoSum, TAOCP vol. 2, 4.2.2): hi + x = s + e
@@ -489,8 +494,8 @@ template <bool CG> __device__ __forceinline__ float ld1(const float* p) { return
 
 template <int MODE, bool CG>
 __device__ __forceinline__ float4 fetch_bar(int j, const float4& own, const float4* __restrict__ bar,
-                                            const float4* __restrict__ snap) {
-    if (j < 0) return own;
+                                            const float4* __restrict__ snap, const float4* __restrict__ gh) {
+    if (j < 0) return (!CG && j <= -2) ? __ldg(gh + (-2 - j)) : own;
     if (MODE != M_INMEM && (j & BORDER)) return snap[j & POS_MASK];
     return ld4<CG>(bar + j);
 }
@@ -526,13 +531,16 @@ struct DualLd { float4 b, B0, B2, B4, P, Q; float q5; };
 template <int MODE, bool CG>
 __device__ __forceinline__ void dual_load(const IterArgs& a, int p, DualLd& L) {
     L.b = ld4<CG>(a.bar + p);
-    const int j0 = __ldg(a.nb + p), j2 = __ldg(a.nb + 2 * a.npos + p), j4 = __ldg(a.nb + 4 * a.npos + p);
+    const bool g = !CG && a.dnb;
+    const int* jb = g ? a.dnb + (p - a.o) : a.nb + p;
+    const int js = g ? a.n : 2 * a.npos;
+    const int j0 = __ldg(jb), j2 = __ldg(jb + js), j4 = __ldg(jb + 2 * js);
     L.P = ld4<CG>(a.P4 + p);
     L.Q = ld4<CG>(a.Q4 + p);
     L.q5 = ld1<CG>(a.Q1 + p);
-    L.B0 = fetch_bar<MODE, CG>(j0, L.b, a.bar, a.snap);
-    L.B2 = fetch_bar<MODE, CG>(j2, L.b, a.bar, a.snap);
-    L.B4 = fetch_bar<MODE, CG>(j4, L.b, a.bar, a.snap);
+    L.B0 = fetch_bar<MODE, CG>(j0, L.b, a.bar, a.snap, a.dgh);
+    L.B2 = fetch_bar<MODE, CG>(j2, L.b, a.bar, a.snap, a.dgh);
+    L.B4 = fetch_bar<MODE, CG>(j4, L.b, a.bar, a.snap, a.dgh);
 }
 
 template <bool RES>
@@ -714,7 +722,9 @@ __device__ __forceinline__ void prefetch_group(const IterArgs& a, int q0, int en
         else if (lane < 8) line = in4 ? a.P4 + q0 + 8 * k4 : nullptr;
         else if (lane < 12) line = in4 ? a.Q4 + q0 + 8 * k4 : nullptr;
         else if (lane == 12) line = a.Q1 + q0;
-        else if (lane < 16) line = a.nb + (size_t)(2 * (lane - 13)) * a.npos + q0;
+        else if (lane < 16)
+            line = a.dnb ? a.dnb + (size_t)(lane - 13) * a.n + (q0 - a.o)
+                         : a.nb + (size_t)(2 * (lane - 13)) * a.npos + q0;
     } else {
         if (lane < 4) line = in4 ? a.uv + q0 + 8 * k4 : nullptr;
         else if (lane < 8) line = in4 ? a.P4 + q0 + 8 * k4 : nullptr;
@@ -1113,6 +1123,55 @@ __global__ void k_ghost_fill(int o, int cnt, int npos, const int* __restrict__ n
     gh[e] = f == 0 ? make_float4(A.x, A.w, B.z, B.w)
           : f == 1 ? make_float4(A.y, B.x, B.z, Q1[j])
                    : make_float4(A.z, B.y, B.w, Q1[j]);
+}
+
+// The dual sweep's ghosts: +x/+y/+z faces whose neighbour is on another level
+// (coarser: finished; deeper: not started) and not a frozen border cube; the
+// copy is the neighbour's bar.  Built only on levels of at least
+// DUAL_GHOST_MIN cubes whose next deeper level is at least twice as large,
+// where many faces have a deeper neighbour: on the finest levels the dual's bar
+// gathers already come from L2, and on smaller levels, which are bound by
+// latency, the redirect only adds work.
+static constexpr int DUAL_GHOST_MIN = 262144;
+template <int MODE>
+__device__ __forceinline__ bool dual_ghost_face(int raw, int o, int lend) {
+    if (raw < 0 || (MODE == M_STREAM && (raw & BORDER))) return false;
+    const int j = raw & POS_MASK;
+    return j < o || j >= lend;
+}
+
+template <int MODE>
+__global__ void k_ghost_mark_dual(int o, int cnt, int npos, const int* __restrict__ nb, const int* __restrict__ par,
+                                  int* __restrict__ mark) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * (int64_t)cnt) return;
+    const int f = int(t / cnt), i = int(t - (int64_t)f * cnt), p = o + i;
+    const int* nbf = nb + (size_t)(2 * f) * npos;
+    const int raw = nbf[p];
+    mark[t] = dual_ghost_face<MODE>(raw, o, o + cnt) && ghost_first(nbf, par, o, p, raw) == p;
+}
+
+template <int MODE>
+__global__ void k_ghost_fill_dual(int o, int cnt, int npos, const int* __restrict__ nb, const int* __restrict__ par,
+                                  const int* __restrict__ mark, const int* __restrict__ ids,
+                                  const float4* __restrict__ bar, int* __restrict__ dnb, float4* __restrict__ gh) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * (int64_t)cnt) return;
+    const int f = int(t / cnt), i = int(t - (int64_t)f * cnt), p = o + i;
+    const int* nbf = nb + (size_t)(2 * f) * npos;
+    const int raw = nbf[p];
+    if (!dual_ghost_face<MODE>(raw, o, o + cnt)) {
+        dnb[t] = raw;
+        return;
+    }
+    const int q = ghost_first(nbf, par, o, p, raw);
+    if (!mark[(int64_t)f * cnt + (q - o)]) {
+        dnb[t] = raw;
+        return;
+    }
+    const int e = ids[(int64_t)f * cnt + (q - o)];
+    dnb[t] = -2 - e;
+    if (q == p) gh[e] = bar[raw & POS_MASK];
 }
 
 // Streaming semantics, tolerance-stopped solve: at each level's start a leaf's
@@ -3251,12 +3310,21 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
     }
     // coarser-neighbour ghost tables for levels run by the per-launch sweep
     // schedules (in-memory and streaming semantics, state on the device)
-    int gmax = 0;
+    int gmax = 0, dmax = 0;
+    std::vector<char> dual_ghosts(levels.size(), 0);
     if (mode != M_OC && !paged)
-        for (const Level& lvl : levels)
-            if (lvl.cnt >= GHOST_MIN && lvl.cnt <= GHOST_MAX) gmax = std::max(gmax, lvl.cnt);
-    int *g_pnb = nullptr, *g_mark = nullptr, *g_ids = nullptr, *g_sums = nullptr;
-    float4* g_val = nullptr;
+        for (size_t k = 0; k < levels.size(); ++k) {
+            const Level& lvl = levels[k];
+            if (lvl.cnt < GHOST_MIN || lvl.cnt > GHOST_MAX) continue;
+            gmax = std::max(gmax, lvl.cnt);
+            if (lvl.cnt >= DUAL_GHOST_MIN && k + 1 < levels.size() && levels[k + 1].d == lvl.d + 1 &&
+                levels[k + 1].cnt >= 2ll * lvl.cnt) {
+                dual_ghosts[k] = 1;
+                dmax = std::max(dmax, lvl.cnt);
+            }
+        }
+    int *g_pnb = nullptr, *g_mark = nullptr, *g_ids = nullptr, *g_sums = nullptr, *g_dnb = nullptr;
+    float4 *g_val = nullptr, *g_dval = nullptr;
     if (gmax > 0) {
         g_pnb = (int*)B(B_G_PNB, 12ull * gmax);
         g_val = (float4*)B(B_G_VAL, 48ull * gmax);
@@ -3264,6 +3332,11 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
         g_ids = (int*)B(B_G_IDS, 12ull * gmax);
         g_sums = (int*)B(B_G_SUMS, 4ull * scan_sums_len(3ll * gmax));
         if (!g_pnb || !g_val || !g_mark || !g_ids || !g_sums) return TGVG_ERR_NOMEM;
+        if (dmax > 0) {
+            g_dnb = (int*)B(B_G_DNB, 12ull * dmax);
+            g_dval = (float4*)B(B_G_DVAL, 48ull * dmax);
+            if (!g_dnb || !g_dval) return TGVG_ERR_NOMEM;
+        }
     }
     const int nlv = std::min<int>((int)levels.size(), TGVG_MAX_LEVELS);
     double* lv_res = nullptr;
@@ -3338,6 +3411,22 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                     k_ghost_fill<M_INMEM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark, g_ids, P4, Q4,
                                                                        Q1, g_pnb, g_val);
                 TGVG_LAUNCHED(ctx);
+                if (dual_ghosts[k]) {  // mark and ids are reused: the primal fill above has read them
+                    if (mode == M_STREAM)
+                        k_ghost_mark_dual<M_STREAM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark);
+                    else
+                        k_ghost_mark_dual<M_INMEM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark);
+                    TGVG_LAUNCHED(ctx);
+                    const int rc2 = scan_exclusive_async(ctx, g_mark, 3ll * cnt, g_ids, g_sums);
+                    if (rc2) return rc2;
+                    if (mode == M_STREAM)
+                        k_ghost_fill_dual<M_STREAM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark, g_ids,
+                                                                                 bar, g_dnb, g_dval);
+                    else
+                        k_ghost_fill_dual<M_INMEM><<<gb, 256, 0, ctx->stream>>>(o, cnt, n, nb, par, g_mark, g_ids,
+                                                                                bar, g_dnb, g_dval);
+                    TGVG_LAUNCHED(ctx);
+                }
             }
             // Every slot's iteration count starts at the full count: the fused
             // schedules' settle step reads it in fixed-count solves too, so a
@@ -3372,6 +3461,8 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                 a.iters_run = iters_run; a.resid = resid;
                 a.pnb = ghosts ? g_pnb : nullptr;
                 a.gh = ghosts ? g_val : nullptr;
+                a.dnb = ghosts && dual_ghosts[k] ? g_dnb : nullptr;
+                a.dgh = ghosts && dual_ghosts[k] ? g_dval : nullptr;
                 set_fuse(Ld);
                 const int rc = run_unit(ctx, mode, a, iters, stop, Ld == t_level, u.cfg, &used_cfg);
                 if (rc) { nvtxRangePop(); return rc; }
@@ -3419,7 +3510,7 @@ int tgv_solve_dev(tgvg_ctx* ctx, const tgvg_cube* d_cubes, const uint32_t* d_his
                               fused_ok ? fz0.barB : nullptr, fused_ok ? fz0.P4B : nullptr,
                               fused_ok ? fz0.Q4B : nullptr, fused_ok ? fz0.Q1B : nullptr,
                               fused_ok ? fz0.slot : nullptr, fused_ok ? fz0.halo : nullptr,
-                              g_pnb, g_val, g_mark, g_ids, g_sums};
+                              g_pnb, g_val, g_mark, g_ids, g_sums, g_dnb, g_dval};
         for (const void* q : ptrs) key.push_back((uint64_t)(uintptr_t)q);
         for (const Level& lvl : levels) {
             key.push_back(((uint64_t)lvl.d << 32) | (uint32_t)lvl.o);
